@@ -1,0 +1,332 @@
+"""Python mirror of the reference's hot-path interface, backed by the GB300
+C ABI (include/asmooth_gb300.h).
+
+Particles are numpy structured arrays with the reference's ``struct Particle``
+layout (basic_types.h:10-15): ``x`` float32[3], ``v`` float32[3], ``dens``,
+``rk`` float32 and ``igrp`` int32, 36 bytes per record.  The functions keep the
+reference's names and argument meaning:
+
+  neighbor_search        KDTree::construct + neighbor_search loop
+                         (clumping_tree_main.cpp:390-395, :418-430)
+  assign_on_mesh         clear_mesh + assign_on_mesh (coarse_mesh.cpp:24-127)
+  assign_on_global_mesh  periodic variant (global_mesh.cpp:25-123)
+  assign_on_density_mesh n-only variant (coarse_mesh.cpp:212-269)
+  mesh_total             FP64 totals (coarse_mesh.cpp:35-43)
+  normalise_mesh         write_mesh_separate normalisation (coarse_mesh.cpp:158-171)
+  group_fof, remove_small_groups (fof.cpp:34-166)
+  mark_halo_particles    SO-halo loop (clumping_tree_main.cpp:465-485)
+
+Where the reference asserts or aborts, these raise :class:`AsmoothError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+PARTICLE_DTYPE = np.dtype([("x", "<f4", (3,)), ("v", "<f4", (3,)), ("dens", "<f4"),
+                           ("rk", "<f4"), ("igrp", "<i4")])
+HALO_DTYPE = np.dtype([("x", "<f4", (3,)), ("r", "<f4"), ("mass", "<f4")])
+assert PARTICLE_DTYPE.itemsize == 36 and HALO_DTYPE.itemsize == 20
+
+ASG_OK = 0
+ASG_ERR_ARG, ASG_ERR_CUDA, ASG_ERR_NOMEM, ASG_ERR_FEW, ASG_ERR_ZERO_RK = -1, -2, -3, -4, -5
+ASG_ERR_NONFINITE, ASG_ERR_STACK, ASG_ERR_TIES, ASG_ERR_RANGE, ASG_ERR_STATE = -6, -7, -8, -9, -10
+ASG_ERR_UNIONFIND = -11
+
+
+class AsmoothError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+def make_particles(x, v=None, dens=None, rk=None, igrp=None) -> np.ndarray:
+    """Build a Particle record array (the reader's state: dens = rk = igrp = 0)."""
+    x = np.asarray(x, np.float32)
+    p = np.zeros(x.shape[0], PARTICLE_DTYPE)
+    p["x"] = x
+    if v is not None:
+        p["v"] = v
+    if dens is not None:
+        p["dens"] = dens
+    if rk is not None:
+        p["rk"] = rk
+    if igrp is not None:
+        p["igrp"] = igrp
+    return p
+
+
+def make_halos(x, r, mass) -> np.ndarray:
+    h = np.zeros(len(r), HALO_DTYPE)
+    h["x"] = np.asarray(x, np.float32).reshape(-1, 3)
+    h["r"] = r
+    h["mass"] = mass
+    return h
+
+
+def _ptr(a) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
+
+
+def _check_particles(p: np.ndarray) -> np.ndarray:
+    if not isinstance(p, np.ndarray) or p.dtype != PARTICLE_DTYPE or not p.flags.c_contiguous:
+        raise TypeError("particles must be a C-contiguous array of PARTICLE_DTYPE")
+    return p
+
+
+class Context:
+    """One library context: a CUDA stream and device buffers on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.asg_create(C.byref(h), int(device))
+        if rc != ASG_OK:
+            raise AsmoothError(rc, self.lib.asg_strerror(rc).decode())
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.asg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ok(self, rc: int):
+        if rc != ASG_OK:
+            msg = self.lib.asg_strerror(rc).decode()
+            detail = self.lib.asg_last_error(self.h).decode()
+            raise AsmoothError(rc, f"{msg}: {detail}")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.lib.asg_kernel_launches(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.asg_stream(self.h) or 0)
+
+    def set_timing(self, enable: bool = True):
+        self._ok(self.lib.asg_set_timing(self.h, int(bool(enable))))
+
+    def phase_ms(self) -> dict:
+        ms = np.zeros(_lib.NPHASES, np.float64)
+        self._ok(self.lib.asg_phase_ms(self.h, _ptr(ms)))
+        return {self.lib.asg_phase_name(i).decode(): float(ms[i]) for i in range(_lib.NPHASES)}
+
+    def measure_fp32_peak(self) -> float:
+        t = C.c_double(0.0)
+        self._ok(self.lib.asg_measure_fp32_peak(self.h, C.byref(t)))
+        return t.value
+
+    # ---- reference-shaped calls (host arrays, in place) -------------------------
+    def neighbor_search(self, p: np.ndarray, left: float, right: float) -> np.ndarray:
+        _check_particles(p)
+        self._ok(self.lib.asg_neighbor_search(self.h, _ptr(p), len(p), left, right))
+        return p
+
+    def assign_on_meshes(self, p: np.ndarray, boxsize: float, ncs, sign: int = 1,
+                         periodic: bool = False, coords=(0, 0, 0)):
+        _check_particles(p)
+        ncs = [int(nc) for nc in ncs]
+        meshes = [np.zeros(6 * nc ** 3, np.float32) for nc in ncs]
+        arr = (C.c_void_p * len(ncs))(*[m.ctypes.data for m in meshes])
+        nca = np.asarray(ncs, np.int32)
+        co = np.asarray(coords, np.int32)
+        tot = np.zeros(2 * len(ncs), np.float64)
+        self._ok(self.lib.asg_assign_on_meshes(self.h, _ptr(p), len(p), boxsize, _ptr(nca), len(ncs),
+                                               int(sign), int(bool(periodic)), _ptr(co), arr,
+                                               _ptr(tot)))
+        return meshes, tot.reshape(-1, 2)
+
+    def assign_on_mesh(self, p: np.ndarray, boxsize: float, nc: int, sign: int = 1):
+        meshes, tot = self.assign_on_meshes(p, boxsize, [nc], sign)
+        return meshes[0], tot[0]
+
+    def assign_on_global_mesh(self, p: np.ndarray, boxsize: float, nc: int, sign: int = 1,
+                              coords=(0, 0, 0)):
+        meshes, tot = self.assign_on_meshes(p, boxsize, [nc], sign, periodic=True, coords=coords)
+        return meshes[0], tot[0]
+
+    def assign_on_density_mesh(self, p: np.ndarray, boxsize: float, nc: int, sign: int = 1):
+        _check_particles(p)
+        mesh = np.zeros(nc ** 3, np.float32)
+        self._ok(self.lib.asg_assign_on_density_mesh(self.h, _ptr(p), len(p), boxsize, int(nc),
+                                                     int(sign), _ptr(mesh)))
+        return mesh
+
+    def normalise_mesh(self, mesh: np.ndarray, nc: int, boxsize: float) -> np.ndarray:
+        m = np.ascontiguousarray(mesh, np.float32).copy()
+        self._ok(self.lib.asg_normalise_mesh(self.h, _ptr(m), int(nc), boxsize))
+        return m
+
+    def group_fof(self, p: np.ndarray, left: float, right: float, ll: float) -> int:
+        _check_particles(p)
+        ng = C.c_int(0)
+        self._ok(self.lib.asg_group_fof(self.h, _ptr(p), len(p), left, right, ll, C.byref(ng)))
+        return ng.value
+
+    def remove_small_groups(self, p: np.ndarray, ngrp: int) -> int:
+        _check_particles(p)
+        nh = C.c_int(0)
+        self._ok(self.lib.asg_remove_small_groups(self.h, _ptr(p), len(p), int(ngrp), C.byref(nh)))
+        return nh.value
+
+    def mark_halo_particles(self, p: np.ndarray, halos: np.ndarray, left: float, right: float):
+        _check_particles(p)
+        halos = np.ascontiguousarray(halos, HALO_DTYPE)
+        nph = C.c_long(0)
+        mh = C.c_double(0.0)
+        self._ok(self.lib.asg_mark_halo_particles(self.h, _ptr(p), len(p), _ptr(halos), len(halos),
+                                                  left, right, C.byref(nph), C.byref(mh)))
+        return nph.value, mh.value
+
+    def smooth(self, p: np.ndarray, left: float, right: float, boxsize: float, ncs,
+               sign: int = -1, halos: np.ndarray | None = None, meshes=None):
+        """Neighbour search, SO-halo marking and the deposit for every nc in one call."""
+        _check_particles(p)
+        ncs = [int(nc) for nc in ncs]
+        if meshes is None:
+            meshes = [np.zeros(6 * nc ** 3, np.float32) for nc in ncs]
+        arr = (C.c_void_p * len(ncs))(*[m.ctypes.data for m in meshes])
+        nca = np.asarray(ncs, np.int32)
+        tot = np.zeros(2 * len(ncs), np.float64)
+        nh = 0 if halos is None else len(halos)
+        hal = None if halos is None else np.ascontiguousarray(halos, HALO_DTYPE)
+        nph = C.c_long(0)
+        mh = C.c_double(0.0)
+        self._ok(self.lib.asg_smooth(self.h, _ptr(p), len(p), left, right, boxsize, _ptr(hal), nh,
+                                     _ptr(nca), len(ncs), int(sign), arr, _ptr(tot), C.byref(nph),
+                                     C.byref(mh)))
+        return meshes, tot.reshape(-1, 2), nph.value, mh.value
+
+    # ---- staged device-resident interface ------------------------------------------
+    def load_particles(self, p: np.ndarray, left: float, right: float):
+        _check_particles(p)
+        self._ok(self.lib.asg_load_particles(self.h, _ptr(p), len(p), left, right))
+
+    def load_particles_device(self, x_ptr: int, n: int, left: float, right: float, v_ptr: int = 0,
+                              dens_ptr: int = 0, igrp_ptr: int = 0):
+        self._ok(self.lib.asg_load_particles_device(self.h, C.c_void_p(x_ptr), C.c_void_p(v_ptr),
+                                                    C.c_void_p(dens_ptr), C.c_void_p(igrp_ptr),
+                                                    int(n), left, right))
+
+    def run_neighbor_search(self):
+        self._ok(self.lib.asg_run_neighbor_search(self.h))
+
+    def run_mark_halos(self, halos: np.ndarray):
+        halos = np.ascontiguousarray(halos, HALO_DTYPE)
+        nph = C.c_long(0)
+        mh = C.c_double(0.0)
+        self._ok(self.lib.asg_run_mark_halos(self.h, _ptr(halos), len(halos), C.byref(nph),
+                                             C.byref(mh)))
+        return nph.value, mh.value
+
+    def run_fof(self, ll: float) -> int:
+        ng = C.c_int(0)
+        self._ok(self.lib.asg_run_fof(self.h, ll, C.byref(ng)))
+        return ng.value
+
+    def run_remove_small_groups(self, ngrp: int) -> int:
+        nh = C.c_int(0)
+        self._ok(self.lib.asg_run_remove_small_groups(self.h, int(ngrp), C.byref(nh)))
+        return nh.value
+
+    def run_deposit(self, boxsize: float, ncs, sign: int = -1, periodic: bool = False,
+                    coords=(0, 0, 0), density_only: bool = False, want_totals: bool = True):
+        ncs = [int(nc) for nc in ncs]
+        nca = np.asarray(ncs, np.int32)
+        co = np.asarray(coords, np.int32)
+        tot = np.zeros(2 * len(ncs), np.float64) if want_totals else None
+        self._ok(self.lib.asg_run_deposit(self.h, boxsize, _ptr(nca), len(ncs), int(sign),
+                                          int(bool(periodic)), _ptr(co), int(bool(density_only)),
+                                          _ptr(tot)))
+        return None if tot is None else tot.reshape(-1, 2)
+
+    def run_normalise(self, k: int):
+        self._ok(self.lib.asg_run_normalise(self.h, int(k)))
+
+    def mesh_device_ptr(self, k: int) -> int:
+        return int(self.lib.asg_mesh_device(self.h, int(k)) or 0)
+
+    def copy_mesh(self, k: int, words: int) -> np.ndarray:
+        m = np.zeros(words, np.float32)
+        self._ok(self.lib.asg_copy_mesh(self.h, int(k), _ptr(m)))
+        return m
+
+    def store_particles(self, p: np.ndarray) -> np.ndarray:
+        _check_particles(p)
+        self._ok(self.lib.asg_store_particles(self.h, _ptr(p)))
+        return p
+
+    def store_fields_device(self, rk_ptr: int = 0, dens_ptr: int = 0, igrp_ptr: int = 0):
+        self._ok(self.lib.asg_store_fields_device(self.h, C.c_void_p(rk_ptr), C.c_void_p(dens_ptr),
+                                                  C.c_void_p(igrp_ptr)))
+
+    def get_knn(self, n: int):
+        t33 = np.zeros(n, np.float32)
+        idx33 = np.zeros(n, np.int32)
+        self._ok(self.lib.asg_get_knn(self.h, _ptr(t33), _ptr(idx33)))
+        return t33, idx33
+
+
+_DEFAULT: Context | None = None
+
+
+def default_context() -> Context:
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Context(0)
+    return _DEFAULT
+
+
+# module-level names of the reference functions
+def neighbor_search(p, left, right):
+    return default_context().neighbor_search(p, left, right)
+
+
+def assign_on_mesh(p, boxsize, nc, sign=1):
+    return default_context().assign_on_mesh(p, boxsize, nc, sign)
+
+
+def assign_on_global_mesh(p, boxsize, nc, sign=1, coords=(0, 0, 0)):
+    return default_context().assign_on_global_mesh(p, boxsize, nc, sign, coords)
+
+
+def assign_on_density_mesh(p, boxsize, nc, sign=1):
+    return default_context().assign_on_density_mesh(p, boxsize, nc, sign)
+
+
+def mesh_total(mesh, nc) -> float:
+    """FP64 sum of the first nc^3 floats, as mesh_total (coarse_mesh.cpp:35-43)."""
+    return float(np.sum(np.asarray(mesh[: nc ** 3], np.float64)))
+
+
+def normalise_mesh(mesh, nc, boxsize):
+    return default_context().normalise_mesh(mesh, nc, boxsize)
+
+
+def group_fof(p, left, right, ll):
+    return default_context().group_fof(p, left, right, ll)
+
+
+def remove_small_groups(p, ngrp):
+    return default_context().remove_small_groups(p, ngrp)
+
+
+def mark_halo_particles(p, halos, left, right):
+    return default_context().mark_halo_particles(p, halos, left, right)

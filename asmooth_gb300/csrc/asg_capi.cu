@@ -1,0 +1,880 @@
+// asg_capi.cu -- context, device memory and the C ABI (include/asmooth_gb300.h).
+//
+// One context owns one CUDA stream and grow-only device buffers sized for the
+// largest particle set seen.  Each public call validates its arguments, queues
+// its kernels on the context stream, synchronises once at the end and turns
+// the device error word into a status code.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/asmooth_gb300.h"
+#include "asg_common.cuh"
+#include "asg_internal.h"
+
+namespace asg {
+static std::atomic<long long> g_launches{0};
+void count_launches(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+}  // namespace asg
+
+using namespace asg;
+
+namespace {
+
+struct Buf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+struct MeshBuf {
+    Buf mesh, partial;
+    int nc = 0;
+    size_t words = 0;
+};
+
+}  // namespace
+
+struct asg_ctx {
+    int device = 0;
+    cudaStream_t s = nullptr;
+    int* d_err = nullptr;
+    int* h_err = nullptr;  // pinned
+    std::string last;
+
+    // loaded particle set
+    int n = 0;
+    float left = 0.f, right = 0.f;
+    bool loaded = false, knn_done = false, ebox_valid = false;
+    int* perm = nullptr;       // sorted position -> input index
+    uint64_t* keys = nullptr;  // sorted keys
+
+    Buf aos, pos_in, vel_in, igrp_in, rk_in, keys0, keys1, vals0, vals1, sort_tmp;
+    Buf pos, vel, igrp, rk, t33, idx33;
+    Buf meta, parent, leaf_parent, flags, blo, bhi, elo, ehi;
+    Buf uf, minin, mark, scan_tmp, lab_cnt, lab_scan;
+    Buf halos, hcount, hmass;
+    Buf totals, lohi;
+    float mesh_boxsize = 0.0f;
+    std::vector<MeshBuf> meshes;
+
+    // phase timing (CUDA events on the context stream)
+    bool timing = false;
+    double phase_ms[ASG_NPHASES] = {};
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    int open_phase = -1;
+    cudaEvent_t open_ev = nullptr;
+};
+
+namespace {
+
+int fail(asg_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->last = msg;
+    return code;
+}
+
+int cuda_fail(asg_ctx* c, cudaError_t e, const char* where)
+{
+    return fail(c, ASG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                    \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);    \
+    } while (0)
+
+int grow(asg_ctx* ctx, Buf& b, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    if (b.cap >= bytes) return 0;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+    const size_t want = bytes + bytes / 8;
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, ASG_ERR_NOMEM, "cudaMalloc of " + std::to_string(want) + " bytes failed");
+    }
+    b.cap = want;
+    return 0;
+}
+
+template <class T>
+T* P(Buf& b) { return reinterpret_cast<T*>(b.p); }
+
+int device_status(int bits)
+{
+    if (bits & ERR_NONFINITE) return ASG_ERR_NONFINITE;
+    if (bits & ERR_STACK) return ASG_ERR_STACK;
+    if (bits & ERR_FEW) return ASG_ERR_FEW;
+    if (bits & ERR_ZERO_RK) return ASG_ERR_ZERO_RK;
+    if (bits & ERR_TIES) return ASG_ERR_TIES;
+    if (bits & ERR_RANGE) return ASG_ERR_RANGE;
+    if (bits & ERR_UF) return ASG_ERR_UNIONFIND;
+    return ASG_OK;
+}
+
+cudaEvent_t next_event(asg_ctx* ctx)
+{
+    if (ctx->ev_used == ctx->ev_pool.size()) {
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        ctx->ev_pool.push_back(e);
+    }
+    return ctx->ev_pool[ctx->ev_used++];
+}
+
+// phase markers: phase_begin(ctx, p) ... phase_end(ctx) bracket queued kernels
+void phase_begin(asg_ctx* ctx, int phase)
+{
+    if (!ctx->timing) return;
+    ctx->open_phase = phase;
+    ctx->open_ev = next_event(ctx);
+    cudaEventRecord(ctx->open_ev, ctx->s);
+}
+
+void phase_end(asg_ctx* ctx)
+{
+    if (!ctx->timing || ctx->open_phase < 0) return;
+    cudaEvent_t e = next_event(ctx);
+    cudaEventRecord(e, ctx->s);
+    ctx->pending.push_back({ctx->open_phase, {ctx->open_ev, e}});
+    ctx->open_phase = -1;
+}
+
+// wait for the queued work and report device-side and launch errors
+int finish(asg_ctx* ctx, const char* what)
+{
+    CK(cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+    for (auto& pe : ctx->pending) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess)
+            ctx->phase_ms[pe.first] += ms;
+    }
+    ctx->pending.clear();
+    ctx->ev_used = 0;
+    ctx->open_phase = -1;
+    const int bits = *ctx->h_err;
+    if (bits) {
+        CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+        return fail(ctx, device_status(bits),
+                    std::string(what) + ": device error bits " + std::to_string(bits));
+    }
+    return ASG_OK;
+}
+
+TreeView tree_view(asg_ctx* ctx)
+{
+    TreeView t;
+    t.n = ctx->n;
+    t.meta = P<int4>(ctx->meta);
+    t.blo = P<float4>(ctx->blo);
+    t.bhi = P<float4>(ctx->bhi);
+    t.elo = P<float4>(ctx->elo);
+    t.ehi = P<float4>(ctx->ehi);
+    return t;
+}
+
+int alloc_set(asg_ctx* ctx, int n)
+{
+    const size_t N = (size_t)n, M = (size_t)(n > 1 ? n - 1 : 1);
+    int r = 0;
+    r |= grow(ctx, ctx->pos_in, 16 * N);
+    r |= grow(ctx, ctx->vel_in, 16 * N);
+    r |= grow(ctx, ctx->igrp_in, 4 * N);
+    r |= grow(ctx, ctx->rk_in, 4 * N);
+    r |= grow(ctx, ctx->keys0, 8 * N);
+    r |= grow(ctx, ctx->keys1, 8 * N);
+    r |= grow(ctx, ctx->vals0, 4 * N);
+    r |= grow(ctx, ctx->vals1, 4 * N);
+    r |= grow(ctx, ctx->sort_tmp, radix_sort_temp_bytes(n));
+    r |= grow(ctx, ctx->pos, 16 * N);
+    r |= grow(ctx, ctx->vel, 16 * N);
+    r |= grow(ctx, ctx->igrp, 4 * N);
+    r |= grow(ctx, ctx->rk, 4 * N);
+    r |= grow(ctx, ctx->t33, 4 * N);
+    r |= grow(ctx, ctx->idx33, 4 * N);
+    r |= grow(ctx, ctx->meta, 16 * M);
+    r |= grow(ctx, ctx->parent, 4 * M);
+    r |= grow(ctx, ctx->leaf_parent, 4 * N);
+    r |= grow(ctx, ctx->flags, 4 * M);
+    r |= grow(ctx, ctx->blo, 16 * M);
+    r |= grow(ctx, ctx->bhi, 16 * M);
+    r |= grow(ctx, ctx->elo, 16 * M);
+    r |= grow(ctx, ctx->ehi, 16 * M);
+    return r ? ASG_ERR_NOMEM : 0;
+}
+
+// sort the staged SoA (pos_in/vel_in/igrp_in/rk_in + keys0/vals0) and build the tree
+int build_index(asg_ctx* ctx)
+{
+    const int n = ctx->n;
+    const int cur = radix_sort(P<uint64_t>(ctx->keys0), P<int>(ctx->vals0), P<uint64_t>(ctx->keys1),
+                               P<int>(ctx->vals1), n, 48, ctx->sort_tmp.p, ctx->s);
+    ctx->keys = cur ? P<uint64_t>(ctx->keys1) : P<uint64_t>(ctx->keys0);
+    ctx->perm = cur ? P<int>(ctx->vals1) : P<int>(ctx->vals0);
+    launch_gather_sorted(ctx->perm, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
+                         P<int>(ctx->igrp_in), P<float>(ctx->rk_in), n, P<float4>(ctx->pos),
+                         P<float4>(ctx->vel), P<int>(ctx->igrp), P<float>(ctx->rk), ctx->s);
+    launch_build_tree(ctx->keys, n, P<int4>(ctx->meta), P<int>(ctx->parent),
+                      P<int>(ctx->leaf_parent), ctx->s);
+    launch_tree_boxes(P<float4>(ctx->pos), nullptr, n, P<int4>(ctx->meta), P<int>(ctx->parent),
+                      P<int>(ctx->leaf_parent), P<int>(ctx->flags), P<float4>(ctx->blo),
+                      P<float4>(ctx->bhi), ctx->s);
+    phase_end(ctx);
+    ctx->loaded = true;
+    ctx->knn_done = false;
+    ctx->ebox_valid = false;
+    return 0;
+}
+
+int check_bounds(asg_ctx* ctx, int np, float left, float right)
+{
+    if (np <= 0) return fail(ctx, ASG_ERR_ARG, "np must be positive");
+    if (!(left < right) || !std::isfinite(left) || !std::isfinite(right))
+        return fail(ctx, ASG_ERR_ARG, "need finite left < right");
+    return 0;
+}
+
+int ensure_ebox(asg_ctx* ctx)
+{
+    if (ctx->ebox_valid) return 0;
+    phase_begin(ctx, ASG_PH_BOXES);
+    launch_check_rk(P<float>(ctx->rk), ctx->n, ctx->d_err, ctx->s);
+    launch_tree_boxes(P<float4>(ctx->pos), P<float>(ctx->rk), ctx->n, P<int4>(ctx->meta),
+                      P<int>(ctx->parent), P<int>(ctx->leaf_parent), P<int>(ctx->flags),
+                      P<float4>(ctx->elo), P<float4>(ctx->ehi), ctx->s);
+    phase_end(ctx);
+    ctx->ebox_valid = true;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int asg_abi_version(void) { return ASG_ABI_VERSION; }
+
+const char* asg_strerror(int status)
+{
+    switch (status) {
+    case ASG_OK: return "ok";
+    case ASG_ERR_ARG: return "bad argument";
+    case ASG_ERR_CUDA: return "CUDA error";
+    case ASG_ERR_NOMEM: return "device memory allocation failed";
+    case ASG_ERR_FEW: return "fewer than 33 particles reachable by a query";
+    case ASG_ERR_ZERO_RK: return "smoothing length is zero or not finite";
+    case ASG_ERR_NONFINITE: return "non-finite particle position";
+    case ASG_ERR_STACK: return "tree traversal stack overflow";
+    case ASG_ERR_TIES: return "more than 16 exact ties at the 33rd neighbour";
+    case ASG_ERR_RANGE: return "periodic kernel support wider than the mesh";
+    case ASG_ERR_STATE: return "call order: a required previous step is missing";
+    case ASG_ERR_UNIONFIND: return "union-find retry limit reached";
+    default: return "unknown status";
+    }
+}
+
+const char* asg_last_error(asg_ctx* ctx) { return ctx ? ctx->last.c_str() : "no context"; }
+
+int asg_create(asg_ctx** out, int device)
+{
+    if (!out) return ASG_ERR_ARG;
+    *out = nullptr;
+    asg_ctx* ctx = new asg_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        asg_destroy(ctx);
+        return ASG_ERR_CUDA;
+    }
+    *out = ctx;
+    return ASG_OK;
+}
+
+void asg_destroy(asg_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->s) cudaStreamSynchronize(ctx->s);
+    Buf* bufs[] = {&ctx->aos, &ctx->pos_in, &ctx->vel_in, &ctx->igrp_in, &ctx->rk_in,
+                   &ctx->keys0, &ctx->keys1, &ctx->vals0, &ctx->vals1, &ctx->sort_tmp,
+                   &ctx->pos, &ctx->vel, &ctx->igrp, &ctx->rk, &ctx->t33, &ctx->idx33,
+                   &ctx->meta, &ctx->parent, &ctx->leaf_parent, &ctx->flags, &ctx->blo,
+                   &ctx->bhi, &ctx->elo, &ctx->ehi, &ctx->uf, &ctx->minin, &ctx->mark,
+                   &ctx->scan_tmp, &ctx->lab_cnt, &ctx->lab_scan, &ctx->halos, &ctx->hcount,
+                   &ctx->hmass, &ctx->totals, &ctx->lohi};
+    for (Buf* b : bufs)
+        if (b->p) cudaFree(b->p);
+    for (auto& m : ctx->meshes) {
+        if (m.mesh.p) cudaFree(m.mesh.p);
+        if (m.partial.p) cudaFree(m.partial.p);
+    }
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->d_err) cudaFree(ctx->d_err);
+    if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->s) cudaStreamDestroy(ctx->s);
+    delete ctx;
+}
+
+void* asg_stream(asg_ctx* ctx) { return ctx ? (void*)ctx->s : nullptr; }
+long long asg_kernel_launches(asg_ctx*) { return g_launches.load(); }
+
+// ---- staged interface ---------------------------------------------------------
+
+int asg_load_particles(asg_ctx* ctx, const asg_particle* p, int np, float left, float right)
+{
+    if (!ctx || !p) return fail(ctx, ASG_ERR_ARG, "null argument");
+    if (int r = check_bounds(ctx, np, left, right)) return r;
+    CK(cudaSetDevice(ctx->device));
+    if (int r = alloc_set(ctx, np)) return r;
+    if (int r = grow(ctx, ctx->aos, sizeof(asg_particle) * (size_t)np)) return r;
+    ctx->n = np;
+    ctx->left = left;
+    ctx->right = right;
+    CK(cudaMemcpyAsync(ctx->aos.p, p, sizeof(asg_particle) * (size_t)np, cudaMemcpyHostToDevice,
+                       ctx->s));
+    phase_begin(ctx, ASG_PH_INDEX);
+    launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
+                      P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
+    launch_morton(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
+                  P<int>(ctx->vals0), ctx->s);
+    build_index(ctx);
+    int r = finish(ctx, "load");
+    if (r) ctx->loaded = false;
+    return r;
+}
+
+int asg_load_particles_device(asg_ctx* ctx, const float* d_x, const float* d_v,
+                              const float* d_dens, const int* d_igrp, int np, float left,
+                              float right)
+{
+    if (!ctx || !d_x) return fail(ctx, ASG_ERR_ARG, "null argument");
+    if (int r = check_bounds(ctx, np, left, right)) return r;
+    CK(cudaSetDevice(ctx->device));
+    if (int r = alloc_set(ctx, np)) return r;
+    ctx->n = np;
+    ctx->left = left;
+    ctx->right = right;
+    phase_begin(ctx, ASG_PH_INDEX);
+    launch_unpack_soa(d_x, d_v, d_dens, d_igrp, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
+                      P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
+    launch_morton(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
+                  P<int>(ctx->vals0), ctx->s);
+    build_index(ctx);
+    int r = finish(ctx, "load_device");
+    if (r) ctx->loaded = false;
+    return r;
+}
+
+static int run_knn(asg_ctx* ctx)
+{
+    const TreeView t = tree_view(ctx);
+    phase_begin(ctx, ASG_PH_KNN);
+    launch_knn_t33(P<float4>(ctx->pos), t, P<float>(ctx->t33), ctx->d_err, ctx->s);
+    phase_end(ctx);
+    phase_begin(ctx, ASG_PH_TIES);
+    launch_knn_ties(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33),
+                    P<float>(ctx->rk), ctx->d_err, ctx->s);
+    phase_end(ctx);
+    ctx->ebox_valid = false;
+    ensure_ebox(ctx);
+    phase_begin(ctx, ASG_PH_DENS);
+    launch_dens_gather(P<float4>(ctx->pos), tree_view(ctx), P<float>(ctx->t33), P<int>(ctx->idx33),
+                       P<float>(ctx->rk), P<float4>(ctx->vel), ctx->s);
+    phase_end(ctx);
+    ctx->knn_done = true;
+    return 0;
+}
+
+int asg_run_neighbor_search(asg_ctx* ctx)
+{
+    if (!ctx) return ASG_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, ASG_ERR_STATE, "no particle set loaded");
+    if (ctx->n < K_NN) return fail(ctx, ASG_ERR_FEW, "fewer than 33 particles");
+    CK(cudaSetDevice(ctx->device));
+    run_knn(ctx);
+    int r = finish(ctx, "neighbor_search");
+    if (r) ctx->knn_done = false;
+    return r;
+}
+
+static int queue_mark(asg_ctx* ctx, const asg_halo* halos, int nh)
+{
+    if (nh <= 0) return 0;
+    if (int r = grow(ctx, ctx->halos, sizeof(asg_halo) * (size_t)nh)) return r;
+    if (int r = grow(ctx, ctx->hcount, sizeof(long long) * (size_t)nh)) return r;
+    if (int r = grow(ctx, ctx->hmass, sizeof(double) * (size_t)nh)) return r;
+    CK(cudaMemcpyAsync(ctx->halos.p, halos, sizeof(asg_halo) * (size_t)nh, cudaMemcpyHostToDevice,
+                       ctx->s));
+    phase_begin(ctx, ASG_PH_HALOS);
+    launch_mark_halos(P<float4>(ctx->pos), tree_view(ctx), P<float>(ctx->halos), nh, ctx->left,
+                      ctx->right, P<int>(ctx->igrp), P<long long>(ctx->hcount),
+                      P<double>(ctx->hmass), ctx->s);
+    phase_end(ctx);
+    return 0;
+}
+
+static int collect_mark(asg_ctx* ctx, int nh, long* np_halo, double* m_halo)
+{
+    long tot = 0;
+    double mh = 0.0;
+    if (nh > 0) {
+        std::vector<long long> cnt((size_t)nh);
+        std::vector<double> m8((size_t)nh);
+        CK(cudaMemcpy(cnt.data(), ctx->hcount.p, sizeof(long long) * (size_t)nh,
+                      cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(m8.data(), ctx->hmass.p, sizeof(double) * (size_t)nh,
+                      cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nh; ++i) {  // halo order, as the reference's serial loop
+            if (cnt[(size_t)i] < 0) return fail(ctx, ASG_ERR_STACK, "mark_halos: stack overflow");
+            tot += (long)cnt[(size_t)i];
+            mh += m8[(size_t)i];
+        }
+    }
+    if (np_halo) *np_halo = tot;
+    if (m_halo) *m_halo = mh;
+    return 0;
+}
+
+int asg_run_mark_halos(asg_ctx* ctx, const asg_halo* halos, int nh, long* np_halo, double* m_halo)
+{
+    if (!ctx || nh < 0 || (nh > 0 && !halos)) return fail(ctx, ASG_ERR_ARG, "bad halo list");
+    if (!ctx->loaded) return fail(ctx, ASG_ERR_STATE, "no particle set loaded");
+    CK(cudaSetDevice(ctx->device));
+    if (int r = queue_mark(ctx, halos, nh)) return r;
+    if (int r = finish(ctx, "mark_halos")) return r;
+    return collect_mark(ctx, nh, np_halo, m_halo);
+}
+
+int asg_run_fof(asg_ctx* ctx, float ll, int* ngroup)
+{
+    if (!ctx || !ngroup || !(ll >= 0.0f) || !std::isfinite(ll))
+        return fail(ctx, ASG_ERR_ARG, "bad FOF arguments");
+    if (!ctx->loaded) return fail(ctx, ASG_ERR_STATE, "no particle set loaded");
+    CK(cudaSetDevice(ctx->device));
+    const int n = ctx->n;
+    if (int r = grow(ctx, ctx->uf, 4 * (size_t)n)) return r;
+    if (int r = grow(ctx, ctx->minin, 4 * (size_t)n)) return r;
+    if (int r = grow(ctx, ctx->mark, 4 * ((size_t)n + 1))) return r;
+    if (int r = grow(ctx, ctx->scan_tmp, scan_temp_bytes((size_t)n + 1))) return r;
+    phase_begin(ctx, ASG_PH_FOF);
+    launch_iota(P<int>(ctx->uf), n, ctx->s);
+    CK(cudaMemsetAsync(ctx->minin.p, 0x7f, 4 * (size_t)n, ctx->s));
+    CK(cudaMemsetAsync(ctx->mark.p, 0, 4 * ((size_t)n + 1), ctx->s));
+    launch_fof_link(P<float4>(ctx->pos), tree_view(ctx), ll, P<int>(ctx->uf), ctx->d_err, ctx->s);
+    launch_fof_finish(P<float4>(ctx->pos), n, P<int>(ctx->uf), P<int>(ctx->minin), P<int>(ctx->mark),
+                      ctx->s);
+    exclusive_scan_u32(P<uint32_t>(ctx->mark), (size_t)n + 1, ctx->scan_tmp.p, ctx->s);
+    launch_fof_label(P<float4>(ctx->pos), n, P<int>(ctx->uf), P<int>(ctx->minin),
+                     P<uint32_t>(ctx->mark), P<int>(ctx->igrp), ctx->s);
+    phase_end(ctx);
+    uint32_t ng = 0;
+    CK(cudaMemcpyAsync(&ng, P<uint32_t>(ctx->mark) + n, 4, cudaMemcpyDeviceToHost, ctx->s));
+    if (int r = finish(ctx, "fof")) return r;
+    *ngroup = (int)ng;
+    return 0;
+}
+
+__global__ static void k_label_range(const int* igrp, int n, int ngrp, int* err)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && (igrp[i] < 0 || igrp[i] > ngrp)) atomicOr(err, ERR_RANGE);
+}
+
+int asg_run_remove_small_groups(asg_ctx* ctx, int ngrp, int* nhalo)
+{
+    if (!ctx || !nhalo || ngrp < 0) return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    if (!ctx->loaded) return fail(ctx, ASG_ERR_STATE, "no particle set loaded");
+    if (ngrp > ctx->n) return fail(ctx, ASG_ERR_ARG, "ngrp larger than the particle count");
+    CK(cudaSetDevice(ctx->device));
+    const int n = ctx->n;
+    const size_t nl = (size_t)ngrp + 2;
+    if (int r = grow(ctx, ctx->lab_cnt, 4 * nl)) return r;
+    if (int r = grow(ctx, ctx->lab_scan, 4 * nl)) return r;
+    if (int r = grow(ctx, ctx->scan_tmp, scan_temp_bytes(nl))) return r;
+    k_label_range<<<(n + 255) / 256, 256, 0, ctx->s>>>(P<int>(ctx->igrp), n, ngrp, ctx->d_err);
+    count_launches(1);
+    if (int r = finish(ctx, "remove_small_groups")) {
+        return fail(ctx, r == ASG_ERR_RANGE ? ASG_ERR_ARG : r, "group labels outside [0, ngrp]");
+    }
+    CK(cudaMemsetAsync(ctx->lab_cnt.p, 0, 4 * nl, ctx->s));
+    launch_count_labels(P<int>(ctx->igrp), n, P<uint32_t>(ctx->lab_cnt), ctx->s);
+    launch_keep_mask(P<uint32_t>(ctx->lab_cnt), ngrp, 20, ctx->s);  // threshold, fof.cpp:107
+    CK(cudaMemsetAsync(P<uint32_t>(ctx->lab_cnt) + ngrp + 1, 0, 4, ctx->s));
+    CK(cudaMemcpyAsync(ctx->lab_scan.p, ctx->lab_cnt.p, 4 * nl, cudaMemcpyDeviceToDevice, ctx->s));
+    exclusive_scan_u32(P<uint32_t>(ctx->lab_scan), nl, ctx->scan_tmp.p, ctx->s);
+    launch_relabel(P<int>(ctx->igrp), n, P<uint32_t>(ctx->lab_scan), P<uint32_t>(ctx->lab_cnt),
+                   ctx->s);
+    uint32_t nh = 0;
+    CK(cudaMemcpyAsync(&nh, P<uint32_t>(ctx->lab_scan) + ngrp + 1, 4, cudaMemcpyDeviceToHost,
+                       ctx->s));
+    if (int r = finish(ctx, "remove_small_groups")) return r;
+    *nhalo = (int)nh;
+    return 0;
+}
+
+static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,
+                         int periodic, const int* coords, int density_only)
+{
+    if (!ncs || n_nc <= 0 || n_nc > MAX_MESHES) return fail(ctx, ASG_ERR_ARG, "1..8 meshes");
+    if (!(boxsize > 0.0f) || !std::isfinite(boxsize)) return fail(ctx, ASG_ERR_ARG, "boxsize");
+    for (int k = 0; k < n_nc; ++k)
+        if (ncs[k] <= 0 || ncs[k] > 1290) return fail(ctx, ASG_ERR_ARG, "nc out of range");
+    ensure_ebox(ctx);
+    if ((int)ctx->meshes.size() < n_nc) ctx->meshes.resize((size_t)n_nc);
+    ctx->mesh_boxsize = boxsize;
+    DepositParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.n_jobs = n_nc;
+    p.boxsize = boxsize;
+    p.sign = sign;
+    p.periodic = periodic ? 1 : 0;
+    p.density_only = density_only ? 1 : 0;
+    for (int d = 0; d < 3; ++d) p.offset[d] = periodic && coords ? boxsize * (float)coords[d] : 0.0f;
+    int tiles = 0;
+    for (int k = 0; k < n_nc; ++k) {
+        MeshBuf& mb = ctx->meshes[(size_t)k];
+        const int nc = ncs[k];
+        const size_t nm = (size_t)nc * nc * nc * (density_only ? 1 : 6);
+        const int tpd = (nc + 7) / 8;
+        if (int r = grow(ctx, mb.mesh, 4 * nm)) return r;
+        if (int r = grow(ctx, mb.partial, 16 * (size_t)tpd * tpd * tpd)) return r;
+        mb.nc = nc;
+        mb.words = nm;
+        MeshJob& j = p.job[k];
+        j.nc = nc;
+        j.dx = boxsize / nc;  // float / int, as coarse_mesh.cpp:58
+        j.ncf = (float)nc;
+        j.tiles[0] = j.tiles[1] = j.tiles[2] = tpd;
+        j.tile_begin = tiles;
+        j.mesh = P<float>(mb.mesh);
+        j.partial = P<double>(mb.partial);
+        tiles += tpd * tpd * tpd;
+    }
+    if (int r = grow(ctx, ctx->totals, 16 * (size_t)n_nc)) return r;
+    phase_begin(ctx, ASG_PH_DEPOSIT);
+    launch_deposit(P<float4>(ctx->pos), P<float4>(ctx->vel), P<int>(ctx->igrp), P<float>(ctx->rk),
+                   tree_view(ctx), p, tiles, ctx->d_err, ctx->s);
+    for (int k = 0; k < n_nc; ++k) {
+        const int tpd = (ncs[k] + 7) / 8;
+        launch_reduce_partials(P<double>(ctx->meshes[(size_t)k].partial), tpd * tpd * tpd,
+                               P<double>(ctx->totals) + 2 * k, ctx->s);
+    }
+    phase_end(ctx);
+    return 0;
+}
+
+int asg_run_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,
+                    int periodic, const int* coords, int density_only, double* totals)
+{
+    if (!ctx) return ASG_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, ASG_ERR_STATE, "no particle set loaded");
+    CK(cudaSetDevice(ctx->device));
+    if (int r = queue_deposit(ctx, boxsize, ncs, n_nc, sign, periodic, coords, density_only))
+        return r;
+    if (totals)
+        CK(cudaMemcpyAsync(totals, ctx->totals.p, 16 * (size_t)n_nc, cudaMemcpyDeviceToHost, ctx->s));
+    return finish(ctx, "deposit");
+}
+
+float* asg_mesh_device(asg_ctx* ctx, int k)
+{
+    if (!ctx || k < 0 || k >= (int)ctx->meshes.size()) return nullptr;
+    return P<float>(ctx->meshes[(size_t)k].mesh);
+}
+
+int asg_copy_mesh(asg_ctx* ctx, int k, float* host)
+{
+    if (!ctx || !host || k < 0 || k >= (int)ctx->meshes.size() || !ctx->meshes[(size_t)k].nc)
+        return fail(ctx, ASG_ERR_ARG, "no such mesh");
+    CK(cudaMemcpyAsync(host, ctx->meshes[(size_t)k].mesh.p, 4 * ctx->meshes[(size_t)k].words,
+                       cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return 0;
+}
+
+int asg_run_normalise(asg_ctx* ctx, int k)
+{
+    if (!ctx || k < 0 || k >= (int)ctx->meshes.size() || !ctx->meshes[(size_t)k].nc)
+        return fail(ctx, ASG_ERR_ARG, "no such mesh");
+    const MeshBuf& mb = ctx->meshes[(size_t)k];
+    if (mb.words != 6 * (size_t)mb.nc * mb.nc * mb.nc)
+        return fail(ctx, ASG_ERR_STATE, "density-only mesh has no c/v channels");
+    CK(cudaSetDevice(ctx->device));
+    const float vol = std::pow(ctx->mesh_boxsize / mb.nc, 3.0f);  // coarse_mesh.cpp:151
+    launch_normalise(P<float>(ctx->meshes[(size_t)k].mesh), mb.nc, vol, ctx->s);
+    return finish(ctx, "normalise");
+}
+
+int asg_store_particles(asg_ctx* ctx, asg_particle* p)
+{
+    if (!ctx || !p) return fail(ctx, ASG_ERR_ARG, "null argument");
+    if (!ctx->loaded) return fail(ctx, ASG_ERR_STATE, "no particle set loaded");
+    CK(cudaSetDevice(ctx->device));
+    if (int r = grow(ctx, ctx->aos, sizeof(asg_particle) * (size_t)ctx->n)) return r;
+    launch_pack_aos(ctx->perm, P<float4>(ctx->pos), P<float4>(ctx->vel), P<float>(ctx->rk), nullptr,
+                    P<int>(ctx->igrp), ctx->n, ctx->aos.p, ctx->s);
+    CK(cudaMemcpyAsync(p, ctx->aos.p, sizeof(asg_particle) * (size_t)ctx->n, cudaMemcpyDeviceToHost,
+                       ctx->s));
+    return finish(ctx, "store");
+}
+
+__global__ static void k_dens_of(const float4* vel, int n, float* dens)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dens[i] = vel[i].w;
+}
+
+int asg_store_fields_device(asg_ctx* ctx, float* d_rk, float* d_dens, int* d_igrp)
+{
+    if (!ctx) return ASG_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, ASG_ERR_STATE, "no particle set loaded");
+    CK(cudaSetDevice(ctx->device));
+    float* dens_s = nullptr;
+    if (d_dens) {  // sorted dens lives in vel.w: stage it in a scratch array
+        if (int r = grow(ctx, ctx->lab_scan, 4 * (size_t)ctx->n)) return r;
+        dens_s = P<float>(ctx->lab_scan);
+        k_dens_of<<<(ctx->n + 255) / 256, 256, 0, ctx->s>>>(P<float4>(ctx->vel), ctx->n, dens_s);
+        count_launches(1);
+    }
+    launch_scatter_fields(ctx->perm, P<float>(ctx->rk), dens_s, P<int>(ctx->igrp), ctx->n, d_rk,
+                          d_dens, d_igrp, ctx->s);
+    return finish(ctx, "store_fields");
+}
+
+int asg_get_knn(asg_ctx* ctx, float* t33, int* idx33)
+{
+    if (!ctx) return ASG_ERR_ARG;
+    if (!ctx->knn_done) return fail(ctx, ASG_ERR_STATE, "no neighbour search done");
+    CK(cudaSetDevice(ctx->device));
+    const size_t n = (size_t)ctx->n;
+    if (int r = grow(ctx, ctx->uf, 4 * n)) return r;
+    if (int r = grow(ctx, ctx->minin, 4 * n)) return r;
+    launch_scatter_fields(ctx->perm, P<float>(ctx->t33), nullptr, P<int>(ctx->idx33), ctx->n,
+                          P<float>(ctx->uf), nullptr, P<int>(ctx->minin), ctx->s);
+    if (t33) CK(cudaMemcpyAsync(t33, ctx->uf.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
+    if (idx33) CK(cudaMemcpyAsync(idx33, ctx->minin.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
+    return finish(ctx, "get_knn");
+}
+
+// ---- reference-shaped one-shot calls --------------------------------------------
+
+int asg_neighbor_search(asg_ctx* ctx, asg_particle* p, int np, float left, float right)
+{
+    if (np < K_NN && np > 0) return fail(ctx, ASG_ERR_FEW, "fewer than 33 particles");
+    if (int r = asg_load_particles(ctx, p, np, left, right)) return r;
+    if (int r = asg_run_neighbor_search(ctx)) return r;
+    return asg_store_particles(ctx, p);
+}
+
+// load for calls whose reference signature carries no cube bounds: the Morton
+// grid only orders particles, so it spans the particles' own bounding cube,
+// found on the device
+static int load_for_deposit(asg_ctx* ctx, const asg_particle* p, int np)
+{
+    if (!ctx || !p || np <= 0) return fail(ctx, ASG_ERR_ARG, "null argument or np <= 0");
+    CK(cudaSetDevice(ctx->device));
+    if (int r = alloc_set(ctx, np)) return r;
+    if (int r = grow(ctx, ctx->aos, sizeof(asg_particle) * (size_t)np)) return r;
+    if (int r = grow(ctx, ctx->lohi, 8)) return r;
+    ctx->n = np;
+    ctx->left = -INFINITY;
+    ctx->right = INFINITY;
+    CK(cudaMemcpyAsync(ctx->aos.p, p, sizeof(asg_particle) * (size_t)np, cudaMemcpyHostToDevice,
+                       ctx->s));
+    phase_begin(ctx, ASG_PH_INDEX);
+    launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
+                      P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
+    launch_morton(P<float4>(ctx->pos_in), np, 0.0f, 0.0f, P<int>(ctx->lohi), 0,
+                  P<uint64_t>(ctx->keys0), P<int>(ctx->vals0), ctx->s);
+    build_index(ctx);
+    int r = finish(ctx, "load");
+    if (r) ctx->loaded = false;
+    return r;
+}
+
+int asg_assign_on_meshes(asg_ctx* ctx, const asg_particle* p, int np, float boxsize,
+                         const int* ncs, int n_nc, int sign, int periodic, const int* coords,
+                         float* const* meshes, double* totals)
+{
+    if (!meshes) return fail(ctx, ASG_ERR_ARG, "null meshes");
+    if (int r = load_for_deposit(ctx, p, np)) return r;
+    if (int r = asg_run_deposit(ctx, boxsize, ncs, n_nc, sign, periodic, coords, 0, totals))
+        return r;
+    for (int k = 0; k < n_nc; ++k)
+        if (meshes[k])
+            if (int r = asg_copy_mesh(ctx, k, meshes[k])) return r;
+    return 0;
+}
+
+int asg_assign_on_mesh(asg_ctx* ctx, const asg_particle* p, int np, float boxsize, int nc,
+                       int sign, float* mesh, double* totals)
+{
+    float* m[1] = {mesh};
+    return asg_assign_on_meshes(ctx, p, np, boxsize, &nc, 1, sign, 0, nullptr, m, totals);
+}
+
+int asg_assign_on_density_mesh(asg_ctx* ctx, const asg_particle* p, int np, float boxsize,
+                               int nc, int sign, float* mesh)
+{
+    if (!mesh) return fail(ctx, ASG_ERR_ARG, "null mesh");
+    if (int r = load_for_deposit(ctx, p, np)) return r;
+    if (int r = asg_run_deposit(ctx, boxsize, &nc, 1, sign, 0, nullptr, 1, nullptr)) return r;
+    return asg_copy_mesh(ctx, 0, mesh);
+}
+
+int asg_normalise_mesh(asg_ctx* ctx, float* mesh, int nc, float boxsize)
+{
+    if (!ctx || !mesh || nc <= 0 || nc > 1290) return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    const size_t words = 6 * (size_t)nc * nc * nc;
+    if (int r = grow(ctx, ctx->aos, 4 * words)) return r;
+    const float vol = std::pow(boxsize / nc, 3.0f);  // pow(float, float) as coarse_mesh.cpp:151
+    CK(cudaMemcpyAsync(ctx->aos.p, mesh, 4 * words, cudaMemcpyHostToDevice, ctx->s));
+    launch_normalise(P<float>(ctx->aos), nc, vol, ctx->s);
+    CK(cudaMemcpyAsync(mesh, ctx->aos.p, 4 * words, cudaMemcpyDeviceToHost, ctx->s));
+    return finish(ctx, "normalise");
+}
+
+int asg_group_fof(asg_ctx* ctx, asg_particle* p, int np, float left, float right, float ll,
+                  int* ngroup)
+{
+    if (int r = asg_load_particles(ctx, p, np, left, right)) return r;
+    if (int r = asg_run_fof(ctx, ll, ngroup)) return r;
+    return asg_store_particles(ctx, p);
+}
+
+int asg_remove_small_groups(asg_ctx* ctx, asg_particle* p, int np, int ngrp, int* nhalo)
+{
+    if (int r = load_for_deposit(ctx, p, np)) return r;
+    if (int r = asg_run_remove_small_groups(ctx, ngrp, nhalo)) return r;
+    return asg_store_particles(ctx, p);
+}
+
+int asg_mark_halo_particles(asg_ctx* ctx, asg_particle* p, int np, const asg_halo* halos,
+                            int nh, float left, float right, long* np_halo, double* m_halo)
+{
+    if (int r = asg_load_particles(ctx, p, np, left, right)) return r;
+    if (int r = asg_run_mark_halos(ctx, halos, nh, np_halo, m_halo)) return r;
+    return asg_store_particles(ctx, p);
+}
+
+int asg_set_timing(asg_ctx* ctx, int enable)
+{
+    if (!ctx) return ASG_ERR_ARG;
+    ctx->timing = enable != 0;
+    for (double& m : ctx->phase_ms) m = 0.0;
+    return ASG_OK;
+}
+
+int asg_phase_ms(asg_ctx* ctx, double* ms)
+{
+    if (!ctx || !ms) return ASG_ERR_ARG;
+    for (int i = 0; i < ASG_NPHASES; ++i) ms[i] = ctx->phase_ms[i];
+    return ASG_OK;
+}
+
+const char* asg_phase_name(int phase)
+{
+    static const char* names[ASG_NPHASES] = {"index", "knn_t33", "knn_ties", "boxes",
+                                             "dens",  "deposit", "halos",    "fof"};
+    return (phase >= 0 && phase < ASG_NPHASES) ? names[phase] : "?";
+}
+
+__global__ static void k_fma_probe(float* out, int iters, float a, float b)
+{
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3f + k;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], a, b);
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int asg_measure_fp32_peak(asg_ctx* ctx, double* tflops)
+{
+    if (!ctx || !tflops) return ASG_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    if (int r = grow(ctx, ctx->lab_scan, sizeof(float) * (size_t)blocks * threads)) return r;
+    cudaEvent_t e0 = next_event(ctx), e1 = next_event(ctx);
+    k_fma_probe<<<blocks, threads, 0, ctx->s>>>(P<float>(ctx->lab_scan), iters / 8, 0.9999f, 1e-4f);
+    CK(cudaEventRecord(e0, ctx->s));
+    k_fma_probe<<<blocks, threads, 0, ctx->s>>>(P<float>(ctx->lab_scan), iters, 0.9999f, 1e-4f);
+    CK(cudaEventRecord(e1, ctx->s));
+    count_launches(2);
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    ctx->ev_used = 0;
+    const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return finish(ctx, "fp32_peak");
+}
+
+int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, float boxsize,
+               const asg_halo* halos, int nh, const int* ncs, int n_nc, int sign,
+               float* const* meshes, double* totals, long* np_halo, double* m_halo)
+{
+    if (!ctx || !p || (nh > 0 && !halos) || nh < 0) return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    if (np < K_NN) return fail(ctx, np > 0 ? ASG_ERR_FEW : ASG_ERR_ARG, "fewer than 33 particles");
+    if (int r = check_bounds(ctx, np, left, right)) return r;
+    CK(cudaSetDevice(ctx->device));
+    if (int r = alloc_set(ctx, np)) return r;
+    if (int r = grow(ctx, ctx->aos, sizeof(asg_particle) * (size_t)np)) return r;
+    ctx->n = np;
+    ctx->left = left;
+    ctx->right = right;
+    CK(cudaMemcpyAsync(ctx->aos.p, p, sizeof(asg_particle) * (size_t)np, cudaMemcpyHostToDevice,
+                       ctx->s));
+    phase_begin(ctx, ASG_PH_INDEX);
+    launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
+                      P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
+    launch_morton(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
+                  P<int>(ctx->vals0), ctx->s);
+    build_index(ctx);
+    run_knn(ctx);
+    if (int r = queue_mark(ctx, halos, nh)) return r;
+    if (int r = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0)) return r;
+    launch_pack_aos(ctx->perm, P<float4>(ctx->pos), P<float4>(ctx->vel), P<float>(ctx->rk), nullptr,
+                    P<int>(ctx->igrp), np, ctx->aos.p, ctx->s);
+    CK(cudaMemcpyAsync(p, ctx->aos.p, sizeof(asg_particle) * (size_t)np, cudaMemcpyDeviceToHost,
+                       ctx->s));
+    for (int k = 0; k < n_nc; ++k)
+        if (meshes && meshes[k])
+            CK(cudaMemcpyAsync(meshes[k], ctx->meshes[(size_t)k].mesh.p,
+                               4 * ctx->meshes[(size_t)k].words, cudaMemcpyDeviceToHost, ctx->s));
+    if (totals)
+        CK(cudaMemcpyAsync(totals, ctx->totals.p, 16 * (size_t)n_nc, cudaMemcpyDeviceToHost, ctx->s));
+    if (int r = finish(ctx, "smooth")) return r;
+    return collect_mark(ctx, nh, np_halo, m_halo);
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+// asg_internal.h -- device data layout and kernel launchers shared by the
+// translation units of libasmooth_gb300.so (not part of the public C ABI).
+//
+// Data layout in HBM (one particle set, N particles):
+//   pos   float4[N]  x, y, z, w = input index (int bits)   -- Morton order
+//   vel   float4[N]  vx, vy, vz, dens                        -- Morton order
+//   igrp  int[N]                                             -- Morton order
+//   rk    float[N], t33 float[N], idx33 int[N]               -- Morton order
+// Radix tree over the N sorted Morton keys (Karras 2012), N-1 internal nodes:
+//   meta  int4[N-1]  child0, child1 (>=0 internal, <0 leaf ~i), first, last
+//   blo/bhi float4[N-1]  AABB of the node's particles
+//   elo/ehi float4[N-1]  AABB of the node's [x-h', x+h'] boxes (after kNN)
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace asg {
+
+// process-wide count of kernel launches made by this library
+void count_launches(int k);
+
+struct TreeView {
+    int n;                 // particles (leaves)
+    const int4* meta;      // internal nodes 0..n-2 (root 0); empty when n == 1
+    const float4* blo;
+    const float4* bhi;
+    const float4* elo;
+    const float4* ehi;
+};
+
+// root entry of a traversal: internal node 0, or leaf 0 when n == 1
+__host__ __device__ inline int tree_root(int n) { return n > 1 ? 0 : ~0; }
+
+// ---- index build (asg_index.cu) -------------------------------------------------
+// unpack reference Particle records (36 B), or SoA device arrays, into the
+// staging arrays (input order; pos.w carries the input index)
+void launch_unpack_aos(const void* aos, int n, float4* pos_in, float4* vel_in, int* igrp_in,
+                       float* rk_in, int* err, cudaStream_t s);
+void launch_unpack_soa(const float* x, const float* v, const float* dens, const int* igrp, int n,
+                       float4* pos_in, float4* vel_in, int* igrp_in, float* rk_in, int* err,
+                       cudaStream_t s);
+// 48-bit Morton keys (16 bits per axis) over [left, right)^3, or over the
+// particles' own bounding cube when d_lohi (2 ints of scratch) is given;
+// key_prefix lands in bits 48+ (batched cubes)
+void launch_morton(const float4* pos_in, int n, float left, float right, int* d_lohi,
+                   uint64_t key_prefix, uint64_t* keys, int* vals, cudaStream_t s);
+// stable LSD radix sort of (keys, vals) on the low `bits` bits; ping-pong buffers;
+// returns which buffer (0/1) holds the result
+size_t radix_sort_temp_bytes(int n);
+int radix_sort(uint64_t* keys0, int* vals0, uint64_t* keys1, int* vals1, int n, int bits,
+               void* temp, cudaStream_t s);
+void launch_gather_sorted(const int* perm, const float4* pos_in, const float4* vel_in,
+                          const int* igrp_in, const float* rk_in, int n, float4* pos, float4* vel,
+                          int* igrp, float* rk, cudaStream_t s);
+void launch_iota(int* a, int n, cudaStream_t s);
+// err |= ERR_ZERO_RK when some rk is not a positive finite number
+void launch_check_rk(const float* rk, int n, int* err, cudaStream_t s);
+void launch_build_tree(const uint64_t* keys, int n, int4* meta, int* parent, int* leaf_parent,
+                       cudaStream_t s);
+// bottom-up AABBs; with rk != nullptr also the expanded boxes [x-h', x+h']
+void launch_tree_boxes(const float4* pos, const float* rk, int n, const int4* meta,
+                       const int* parent, const int* leaf_parent, int* flags, float4* lo,
+                       float4* hi, cudaStream_t s);
+// exclusive scan of uint32 counts (in place); temp from scan_temp_bytes
+size_t scan_temp_bytes(size_t n);
+void exclusive_scan_u32(uint32_t* data, size_t n, void* temp, cudaStream_t s);
+
+// ---- neighbour search (asg_knn.cu) -------------------------------------------
+void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, int* err, cudaStream_t s);
+void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int* idx33,
+                     float* rk, int* err, cudaStream_t s);
+// vel[j].w (dens) += the tent weights j receives as one of the 32 nearest
+void launch_dens_gather(const float4* pos, const TreeView& t, const float* t33,
+                        const int* idx33, const float* rk, float4* vel, cudaStream_t s);
+
+// ---- mesh deposit (asg_deposit.cu) ---------------------------------------------
+struct MeshJob {
+    int nc;           // cells per dimension
+    float dx;         // boxsize / nc (host float division, as the reference)
+    float ncf;        // (float)nc
+    int tiles[3];     // tiles per dimension
+    int tile_begin;   // first global tile id of this mesh
+    float* mesh;      // 6*nc^3 floats (reference layout) or nc^3 (density only)
+    double* partial;  // per-tile FP64 partial sums, 2 per tile (n, halo)
+};
+constexpr int MAX_MESHES = 8;
+struct DepositParams {
+    int n_jobs;
+    MeshJob job[MAX_MESHES];
+    float boxsize;
+    int sign;
+    int periodic;
+    float offset[3];  // periodic: rank cube offset
+    int density_only;
+};
+void launch_deposit(const float4* pos, const float4* vel, const int* igrp, const float* rk,
+                    const TreeView& t, const DepositParams& p, int total_tiles, int* err,
+                    cudaStream_t s);
+void launch_reduce_partials(const double* partial, int ntiles, double* out2, cudaStream_t s);
+void launch_normalise(float* mesh, int nc, float vol, cudaStream_t s);
+
+// ---- FOF and SO halos (asg_fof.cu) -----------------------------------------------
+void launch_fof_link(const float4* pos, const TreeView& t, float ll, int* parent, int* err,
+                     cudaStream_t s);
+void launch_fof_finish(const float4* pos, int n, int* parent, int* minin, int* mark,
+                       cudaStream_t s);
+void launch_fof_label(const float4* pos, int n, const int* parent, const int* minin,
+                      const uint32_t* scan, int* igrp_sorted, cudaStream_t s);
+void launch_mark_halos(const float4* pos, const TreeView& t, const float* halos, int nh,
+                       float left, float right, int* igrp, long long* counts, double* mass8,
+                       cudaStream_t s);
+void launch_count_labels(const int* igrp, int n, uint32_t* counts, cudaStream_t s);
+void launch_keep_mask(uint32_t* counts, int ngrp, int threshold, cudaStream_t s);
+void launch_relabel(int* igrp, int n, const uint32_t* scan, const uint32_t* keep, cudaStream_t s);
+
+// ---- output (asg_index.cu) ------------------------------------------------------------
+// write reference Particle records in input order from the sorted fields
+void launch_pack_aos(const int* perm, const float4* pos, const float4* vel, const float* rk,
+                     const float* dens, const int* igrp, int n, void* aos, cudaStream_t s);
+void launch_scatter_fields(const int* perm, const float* rk, const float* dens, const int* igrp,
+                           int n, float* rk_out, float* dens_out, int* igrp_out, cudaStream_t s);
+
+}  // namespace asg

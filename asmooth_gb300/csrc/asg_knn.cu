@@ -1,0 +1,323 @@
+// asg_knn.cu -- k=33 nearest neighbours, smoothing length and particle density
+// (the loop at clumping_tree_main.cpp:418-430 over neighbor_search,
+// nbr_search.cpp:61-127, with KNeighbors k=33 from k_neighbors.h:9-51).
+//
+// Definition implemented (order independent): for query p the neighbour set is
+// the 33 particles with the smallest key (d2, input index), d2 evaluated with
+// the reference's float expression.  rk = sqrtf(d2 of the 33rd); the 32
+// smallest keys (the 33rd excluded, self included) receive the tent weight
+// ker(p, q, 1/rk) in dens.
+//
+// Three warp-bundle traversals of the radix tree; a warp serves the 32
+// consecutive (Morton-ordered) particles of one bundle, one lane per particle,
+// and visits a node when any lane needs it:
+//   k_knn_t33   per-lane sorted top-33 of d2 in registers (min/max network)
+//               -> t33 = 33rd smallest d2 (exact, with multiplicity)
+//   k_knn_ties  exact-radius recount: L = #(d2 < t33), the tied indices
+//               -> idx33 = input index of the 33rd key, rk = sqrtf(t33)
+//   k_dens_gather  each lane is a RECEIVER j and sums ker(q, j) over the
+//               sources q whose 32-set contains j, in traversal order with a
+//               double-float accumulator: deterministic, no atomics.
+#include <climits>
+
+#include "asg_common.cuh"
+#include "asg_internal.h"
+
+namespace asg {
+
+constexpr int KNN_WARPS = 4;
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ void insert33(float (&a)[K_NN], float v)
+{
+#pragma unroll
+    for (int k = 0; k < K_NN; ++k) {
+        const float lo = fminf(a[k], v);
+        v = fmaxf(a[k], v);
+        a[k] = lo;
+    }
+}
+
+// squared distance from the query to a child (point for a leaf child)
+__device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, const TreeView& t,
+                                             int c, float4 q)
+{
+    if (c < 0) {
+        const float4 p = pos[~c];
+        return norm2_rn(q.x, q.y, q.z, p.x, p.y, p.z);
+    }
+    return box_dist2_rn(q.x, q.y, q.z, t.blo[c], t.bhi[c]);
+}
+
+__global__ void __launch_bounds__(KNN_WARPS * 32)
+k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33, int* err)
+{
+    __shared__ int stk[KNN_WARPS][STACK_MAX];
+    __shared__ float4 cand[KNN_WARPS][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = t.n;
+    const int base = (blockIdx.x * KNN_WARPS + warp) * 32;
+    if (base >= n) return;
+    const int q = min(base + lane, n - 1);
+    const float4 xq = pos[q];
+    float a[K_NN];
+#pragma unroll
+    for (int k = 0; k < K_NN; ++k) a[k] = INFINITY;
+
+    int* st = stk[warp];
+    if (lane == 0) st[0] = tree_root(n);
+    int sp = 1;
+    bool overflow = false;
+    __syncwarp();
+    while (sp > 0) {
+        const int node = st[--sp];
+        __syncwarp();
+        int first, last;
+        if (node < 0) {
+            first = last = ~node;
+        } else {
+            const int4 m = t.meta[node];
+            if (m.w - m.z + 1 > LEAF_MAX) {
+                const float d0 = child_dist2(pos, t, m.x, xq);
+                const float d1 = child_dist2(pos, t, m.y, xq);
+                const bool v0 = __any_sync(FULL, d0 < a[K_NN - 1]);
+                const bool v1 = __any_sync(FULL, d1 < a[K_NN - 1]);
+                const bool c0_near = __popc(__ballot_sync(FULL, d0 <= d1)) >= 16;
+                const int nn = c0_near ? m.x : m.y, ff = c0_near ? m.y : m.x;
+                const bool vn = c0_near ? v0 : v1, vf = c0_near ? v1 : v0;
+                if (sp + 2 > STACK_MAX) { overflow = true; break; }
+                if (lane == 0) {
+                    if (vf) st[sp] = ff;
+                    if (vn) st[sp + (vf ? 1 : 0)] = nn;
+                }
+                sp += (vf ? 1 : 0) + (vn ? 1 : 0);
+                __syncwarp();
+                continue;
+            }
+            first = m.z;
+            last = m.w;
+            // thresholds may have shrunk since the push: re-test the bucket
+            const float db = box_dist2_rn(xq.x, xq.y, xq.z, t.blo[node], t.bhi[node]);
+            if (!__any_sync(FULL, db < a[K_NN - 1])) continue;
+        }
+        const int cnt = last - first + 1;
+        if (lane < cnt) cand[warp][lane] = pos[first + lane];
+        __syncwarp();
+        for (int j = 0; j < cnt; ++j) {
+            const float4 c = cand[warp][j];
+            const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
+            const bool take = d2 < a[K_NN - 1];
+            if (__any_sync(FULL, take)) insert33(a, take ? d2 : INFINITY);
+        }
+        __syncwarp();
+    }
+    if (overflow) {
+        if (lane == 0) atomicOr(err, ERR_STACK);
+        return;
+    }
+    if (base + lane < n) {
+        const float v = a[K_NN - 1];
+        t33[base + lane] = v;
+        if (!(v < INFINITY)) atomicOr(err, ERR_FEW);
+        else if (!(v > 0.0f)) atomicOr(err, ERR_ZERO_RK);
+    }
+}
+
+__global__ void __launch_bounds__(KNN_WARPS * 32)
+k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
+           int* __restrict__ idx33, float* __restrict__ rk, int* err)
+{
+    __shared__ int stk[KNN_WARPS][STACK_MAX];
+    __shared__ float4 cand[KNN_WARPS][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = t.n;
+    const int base = (blockIdx.x * KNN_WARPS + warp) * 32;
+    if (base >= n) return;
+    const int q = min(base + lane, n - 1);
+    const float4 xq = pos[q];
+    const float T = t33[q];
+    int nless = 0, neq = 0;
+    int tie[TIE_MAX];
+#pragma unroll
+    for (int k = 0; k < TIE_MAX; ++k) tie[k] = INT_MAX;
+
+    int* st = stk[warp];
+    if (lane == 0) st[0] = tree_root(n);
+    int sp = 1;
+    bool overflow = false;
+    __syncwarp();
+    while (sp > 0) {
+        const int node = st[--sp];
+        __syncwarp();
+        int first, last;
+        if (node < 0) {
+            first = last = ~node;
+        } else {
+            const int4 m = t.meta[node];
+            if (m.w - m.z + 1 > LEAF_MAX) {
+                const bool v0 = __any_sync(FULL, child_dist2(pos, t, m.x, xq) <= T);
+                const bool v1 = __any_sync(FULL, child_dist2(pos, t, m.y, xq) <= T);
+                if (sp + 2 > STACK_MAX) { overflow = true; break; }
+                if (lane == 0) {
+                    if (v1) st[sp] = m.y;
+                    if (v0) st[sp + (v1 ? 1 : 0)] = m.x;
+                }
+                sp += (v0 ? 1 : 0) + (v1 ? 1 : 0);
+                __syncwarp();
+                continue;
+            }
+            first = m.z;
+            last = m.w;
+        }
+        const int cnt = last - first + 1;
+        if (lane < cnt) cand[warp][lane] = pos[first + lane];
+        __syncwarp();
+        for (int j = 0; j < cnt; ++j) {
+            const float4 c = cand[warp][j];
+            const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
+            nless += d2 < T ? 1 : 0;
+            const bool eq = d2 == T;
+            if (__any_sync(FULL, eq)) {
+                neq += eq ? 1 : 0;
+                int v = eq ? __float_as_int(c.w) : INT_MAX;
+#pragma unroll
+                for (int k = 0; k < TIE_MAX; ++k) {
+                    const int lo = min(tie[k], v);
+                    v = max(tie[k], v);
+                    tie[k] = lo;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (overflow) {
+        if (lane == 0) atomicOr(err, ERR_STACK);
+        return;
+    }
+    if (base + lane < n) {
+        const int need = K_NN - nless;  // position of the 33rd key among the ties
+        int r = -1;
+        if (need < 1 || need > neq) atomicOr(err, ERR_FEW);
+        else if (need > TIE_MAX) atomicOr(err, ERR_TIES);
+        else {
+#pragma unroll
+            for (int k = 0; k < TIE_MAX; ++k)
+                if (k == need - 1) r = tie[k];
+        }
+        idx33[base + lane] = r;
+        rk[base + lane] = __fsqrt_rn(T);
+    }
+}
+
+__global__ void __launch_bounds__(KNN_WARPS * 32)
+k_dens_gather(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
+              const int* __restrict__ idx33, const float* __restrict__ rk,
+              float4* __restrict__ vel)
+{
+    __shared__ int stk[KNN_WARPS][STACK_MAX];
+    __shared__ float4 cpos[KNN_WARPS][32];
+    __shared__ float4 cpar[KNN_WARPS][32];  // t33, idx33 bits, hinv, -
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = t.n;
+    const int base = (blockIdx.x * KNN_WARPS + warp) * 32;
+    if (base >= n) return;
+    const int j = min(base + lane, n - 1);
+    const float4 xj = pos[j];
+    const int idx_j = __float_as_int(xj.w);
+    float hi = 0.0f, lo = 0.0f;
+
+    auto inside = [&](float4 l, float4 h) {
+        return xj.x >= l.x && xj.x <= h.x && xj.y >= l.y && xj.y <= h.y && xj.z >= l.z &&
+               xj.z <= h.z;
+    };
+    auto child_in = [&](int c) {
+        if (c < 0) {
+            const float4 p = pos[~c];
+            const float h = __fmul_ru(rk[~c], 1.000001f);
+            return inside(make_float4(__fsub_rd(p.x, h), __fsub_rd(p.y, h), __fsub_rd(p.z, h), 0.f),
+                          make_float4(__fadd_ru(p.x, h), __fadd_ru(p.y, h), __fadd_ru(p.z, h), 0.f));
+        }
+        return inside(t.elo[c], t.ehi[c]);
+    };
+
+    int* st = stk[warp];
+    if (lane == 0) st[0] = tree_root(n);
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+        const int node = st[--sp];
+        __syncwarp();
+        int first, last;
+        if (node < 0) {
+            first = last = ~node;
+        } else {
+            const int4 m = t.meta[node];
+            if (m.w - m.z + 1 > LEAF_MAX) {
+                const bool v0 = __any_sync(FULL, child_in(m.x));
+                const bool v1 = __any_sync(FULL, child_in(m.y));
+                if (sp + 2 > STACK_MAX) break;  // k_knn_t33 already flagged the same tree
+                if (lane == 0) {
+                    if (v1) st[sp] = m.y;
+                    if (v0) st[sp + (v1 ? 1 : 0)] = m.x;
+                }
+                sp += (v0 ? 1 : 0) + (v1 ? 1 : 0);
+                __syncwarp();
+                continue;
+            }
+            first = m.z;
+            last = m.w;
+        }
+        const int cnt = last - first + 1;
+        if (lane < cnt) {
+            const int s = first + lane;
+            cpos[warp][lane] = pos[s];
+            cpar[warp][lane] = make_float4(t33[s], __int_as_float(idx33[s]),
+                                           __fdiv_rn(1.0f, rk[s]), 0.0f);
+        }
+        __syncwarp();
+        for (int k = 0; k < cnt; ++k) {
+            const float4 c = cpos[warp][k];
+            const float4 pr = cpar[warp][k];
+            const float d2 = norm2_rn(c.x, c.y, c.z, xj.x, xj.y, xj.z);
+            const bool member = d2 < pr.x || (d2 == pr.x && idx_j < __float_as_int(pr.y));
+            if (__any_sync(FULL, member)) {
+                const float w = member ? ker_rn(c.x, c.y, c.z, xj.x, xj.y, xj.z, pr.z) : 0.0f;
+                two_sum_acc(hi, lo, w);
+            }
+        }
+        __syncwarp();
+    }
+    // dens accumulates onto the incoming value, as q->dens += ... does
+    if (base + lane < n) {
+        float4 v = vel[base + lane];
+        v.w = __fadd_rn(v.w, __fadd_rn(hi, lo));
+        vel[base + lane] = v;
+    }
+}
+
+static int knn_blocks(int n) { return (n + KNN_WARPS * 32 - 1) / (KNN_WARPS * 32); }
+
+void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, int* err, cudaStream_t s)
+{
+    if (t.n <= 0) return;
+    k_knn_t33<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, err);
+    count_launches(1);
+}
+
+void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int* idx33,
+                     float* rk, int* err, cudaStream_t s)
+{
+    if (t.n <= 0) return;
+    k_knn_ties<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, rk, err);
+    count_launches(1);
+}
+
+void launch_dens_gather(const float4* pos, const TreeView& t, const float* t33,
+                        const int* idx33, const float* rk, float4* vel, cudaStream_t s)
+{
+    if (t.n <= 0) return;
+    k_dens_gather<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, rk, vel);
+    count_launches(1);
+}
+
+}  // namespace asg

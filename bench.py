@@ -1,0 +1,347 @@
+#!/usr/bin/env python3
+"""Benchmark: particles/s of the smoothing hot path (k=32 neighbour search,
+smoothing length, particle density, adaptive deposit at nc = 64, 128, 256) on
+the 256^3-particle NFW-clustered cube of side 512 with its 8-unit periodic
+shell, seeded synthetic data.
+
+One step = index build (Morton sort + radix tree) + neighbour search + dens +
+deposit of all three meshes for one cube.  `value` times steps with inputs
+resident in HBM (CUDA events on the library's stream; L2 is flushed before
+every step and the inputs are larger than L2).  `e2e` times the public C-ABI
+call asg_smooth on pinned host Particle records, host<->device copies
+included (wall clock).  Under torchrun every rank runs an independent replica
+cube (the path does not exchange data); value = total particles / max time.
+
+--impl reference times the reference algorithm on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particles/s, k=32 kNN + SPH deposit at 256^3: mixed vs plain FP32 on 1 GB300"
+WORKLOAD = "cfg2"  # 256^3 particles, side 512, 5000 NFW halos, nc = 64,128,256
+CPU_SAMPLE = ("cfg2", 2)  # same model at 1/8 volume: 128^3 particles, side 256, nc = 32,64,128
+
+
+def env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [c.strip() for c in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def deposit_cells(x, rk, boxsize, ncs):
+    """Sum over particles and meshes of the cells each deposit touches (the
+    reference's cell-range expression, coarse_mesh.cpp:72-75)."""
+    x = x.astype(np.float32)
+    h = rk.astype(np.float32)[:, None]
+    L = np.float32(boxsize)
+    tot = 0
+    for nc in ncs:
+        f = np.float32(nc)
+        lo = np.maximum(0, np.trunc(((x - h) / L) * f).astype(np.int64))
+        hi = np.minimum(nc, 1 + np.trunc(((x + h) / L) * f).astype(np.int64))
+        tot += int(np.prod(np.maximum(hi - lo, 0), axis=1).sum())
+    return tot
+
+
+def cpu_reference_run(nthreads: int, use_ref: bool):
+    """One bounded sample of the workload on the host cores: tree + neighbour
+    search + deposit of the sample's meshes.  Returns (seconds, n_local, kind)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    from asmooth_gb300 import synthetic as syn
+
+    cube, ncs = syn.make_workload(CPU_SAMPLE[0], scale=CPU_SAMPLE[1])
+    ig = np.zeros(cube.n, np.int32)
+    if use_ref and pyoracle.Reference.available(omp=True):
+        R = pyoracle.Reference(omp=True)
+        kind = "reference"
+        t0 = time.perf_counter()
+        rk, dens = R.neighbor_search(cube.x, cube.left, cube.right)  # serial kNN loop in the harness
+        for nc in ncs:
+            R.assign_on_mesh(cube.x, cube.v, dens, rk, ig, cube.boxsize, nc, -1)
+        dt = time.perf_counter() - t0
+        return dt, cube.n_local, kind, 1
+    O = pyoracle.Oracle()
+    t0 = time.perf_counter()
+    rk, dens = O.neighbor_search(cube.x, cube.left, cube.right, nthreads=nthreads)
+    for nc in ncs:
+        O.assign_on_mesh(cube.x, cube.v, dens, rk, ig, cube.boxsize, nc, -1, nthreads=nthreads,
+                         want64=False)
+    dt = time.perf_counter() - t0
+    return dt, cube.n_local, "port", nthreads
+
+
+def run_reference(args):
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build_oracle()
+    times = []
+    kind = "port"
+    n_local = 0
+    for k in range(args.warmup + args.steps):
+        dt, n_local, kind, cores = cpu_reference_run(nthreads, use_ref=False)
+        if k >= args.warmup:
+            times.append(dt)
+    sec = statistics.mean(times)
+    value = n_local / sec
+    sample = (f"{CPU_SAMPLE[0]} model at 1/8 volume: 128^3 particles, side 256, 8-unit shell, "
+              f"nc=32,64,128; tree + neighbour search + deposit per step")
+    line = {
+        "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded NFW-clustered cube)", "impl": "reference",
+        "config": {"workload": f"{WORKLOAD} model, CPU sample: {sample}", "threads": nthreads},
+        "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nthreads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from asmooth_gb300 import api
+    from asmooth_gb300 import synthetic as syn
+
+    seed = 2 + 1000 * rank  # independent replica cube per rank
+    cube, ncs = syn.make_workload(WORKLOAD, seed=seed)
+    n, n_local = cube.n, cube.n_local
+    x_d = torch.from_numpy(cube.x).cuda()
+    v_d = torch.from_numpy(cube.v).cuda()
+    ctx = api.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(512 * 2 ** 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        ctx.load_particles_device(x_d.data_ptr(), n, cube.left, cube.right, v_ptr=v_d.data_ptr())
+        ctx.run_neighbor_search()
+        ctx.run_deposit(cube.boxsize, ncs, sign=-1)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ctx.set_timing(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.kernel_launches
+    total_ms = 0.0
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()  # L2 flush between timed steps (not timed)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - wall0
+    launches = ctx.kernel_launches - launches0
+    phases = ctx.phase_ms()
+    ctx.set_timing(False)
+    clk = clocks.stop()
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_step = float(t.item()) / args.steps
+    value = world * n_local / (ms_step * 1e-3)
+
+    # end to end through the public C ABI: pinned host Particle records in, out
+    rec_bytes = n * api.PARTICLE_DTYPE.itemsize
+    host = torch.empty(rec_bytes, dtype=torch.uint8, pin_memory=True)
+    p = host.numpy().view(api.PARTICLE_DTYPE)
+    p[:] = api.make_particles(cube.x, cube.v)
+    mesh_host = [torch.empty(6 * nc ** 3, dtype=torch.float32, pin_memory=True).numpy() for nc in ncs]
+    for _ in range(max(1, args.warmup)):
+        ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
+    e2e_times = []
+    for _ in range(args.steps):
+        p["dens"] = 0.0
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
+        e2e_times.append(time.perf_counter() - w0)
+    e2e_s = statistics.mean(e2e_times)
+    tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    e2e_value = world * n_local / float(tt.item())
+    d2h = rec_bytes + sum(4 * 6 * nc ** 3 for nc in ncs) + 16 * len(ncs)
+
+    # roofline of the dominant kernel (measured live above)
+    fp32 = ctx.measure_fp32_peak()
+    pk, pk_kind = peaks()
+    cells = deposit_cells(cube.x, p["rk"], cube.boxsize, ncs)
+    alg = {  # algorithmic FP32 flops per step, per phase
+        "knn_t33": 8.0 * 33 * 6 / np.pi * n,  # 8 flops per distance, ~63 candidates per query
+        "dens": 14.0 * 32 * n,                 # 14 flops per tent weight, 32 receivers per query
+        "deposit": 12.0 * cells,               # 12 flops per particle-cell pair
+    }
+    per_step = {k: v / args.steps for k, v in phases.items()}
+    dom = max(("knn_t33", "deposit", "dens"), key=lambda k: per_step.get(k, 0.0))
+    achieved = alg[dom] / (per_step[dom] * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom)
+        except Exception:
+            traffic = None
+    hbm_alg = n * (12 + 8 + 36) + sum(24 * nc ** 3 for nc in ncs)
+    roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": fp32, "unit": "TFLOP/s",
+            "frac": achieved / fp32, "traffic": traffic,
+            "peak_source": "measured FMA-chain kernel on this GPU (no FP32 figure in the peaks file)",
+            "phase_ms_per_step": per_step,
+            "alg_flops_per_step": alg,
+            "step_alg_hbm_bytes": hbm_alg,
+            "step_hbm_gbs_vs_peak": {"achieved": hbm_alg / (ms_step * 1e-3) / 1e9,
+                                     "peak": pk["hbm_gbs"], "peak_kind": pk_kind}}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+
+        pyoracle.build_oracle()
+        nthreads = os.cpu_count() or 1
+        dt, nl, kind, cores = cpu_reference_run(nthreads, use_ref=False)
+        cpu = {"value": nl / dt, "unit": "particles/s", "cores": cores, "kind": kind,
+               "sample": "cfg2 model at 1/8 volume (128^3 particles, side 256, nc=32,64,128), "
+                         "tree + neighbour search + deposit, OpenMP over all host cores"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded NFW-clustered cube in cubep3m layout)",
+        "config": {"workload": "cfg2: 256^3 particles, side 512, 5000 NFW halos, 8-unit periodic "
+                               "shell, k=32, nc=64,128,256, plain FP32 form",
+                   "n_with_shell": n, "n_local": n_local, "parallelism": f"replicas x{world}",
+                   "l2": "flushed before every timed step; inputs larger than L2"},
+        "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": rec_bytes,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

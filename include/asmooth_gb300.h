@@ -1,0 +1,175 @@
+/*
+ * asmooth_gb300.h -- C ABI of the GB300 adaptive-smoothing path.
+ *
+ * Drop-in replacement for the hot path of junkoda/asmooth's clumping_tree:
+ * kd-tree construction, the k=32 (+self) neighbour search with smoothing length
+ * and particle density, the adaptive mesh deposit at several nc, the FP64 mass
+ * totals, the output normalisation, friends-of-friends and SO-halo marking.
+ * The host keeps every buffer; the library owns device memory and one CUDA
+ * stream per context.  All calls are synchronous at return, return an int
+ * status (0 = ASG_OK) and never throw.  One context per host thread; a
+ * context is not thread-safe.
+ *
+ * Particle records are the reference's `struct Particle` (basic_types.h:10-15),
+ * 36 bytes: float x[3], v[3], dens, rk; int igrp.  Halo records are the
+ * reference's `struct Halo` (basic_types.h:17-20): float x[3], r, mass.
+ * Unlike the reference, no call reorders the caller's particle array.
+ */
+#ifndef ASMOOTH_GB300_H
+#define ASMOOTH_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASG_ABI_VERSION 1
+
+typedef struct asg_particle {
+    float x[3], v[3];
+    float dens, rk;
+    int igrp;
+} asg_particle;
+
+typedef struct asg_halo {
+    float x[3];
+    float r, mass;
+} asg_halo;
+
+typedef struct asg_ctx asg_ctx;
+
+enum {
+    ASG_OK = 0,
+    ASG_ERR_ARG = -1,         /* bad argument (null pointer, n or nc out of range) */
+    ASG_ERR_CUDA = -2,        /* CUDA runtime error (see asg_last_error) */
+    ASG_ERR_NOMEM = -3,       /* device allocation failed */
+    ASG_ERR_FEW = -4,         /* fewer than 33 particles can be reached by a query */
+    ASG_ERR_ZERO_RK = -5,     /* 33rd neighbour distance is 0 (>= 33 coincident particles) */
+    ASG_ERR_NONFINITE = -6,   /* NaN or infinite position */
+    ASG_ERR_STACK = -7,       /* tree deeper than the traversal stack */
+    ASG_ERR_TIES = -8,        /* more than 16 particles tied exactly at the 33rd distance */
+    ASG_ERR_RANGE = -9,       /* periodic deposit: kernel support wider than the mesh */
+    ASG_ERR_STATE = -10,      /* call needs a previous step (e.g. deposit before search) */
+    ASG_ERR_UNIONFIND = -11   /* FOF union-find retry limit reached */
+};
+
+/* ---- context ------------------------------------------------------------- */
+int asg_create(asg_ctx** ctx, int device);
+void asg_destroy(asg_ctx* ctx);
+const char* asg_strerror(int status);
+/* text of the last error seen by this context (CUDA message or argument check) */
+const char* asg_last_error(asg_ctx* ctx);
+int asg_abi_version(void);
+
+/* ---- reference-shaped one-shot calls (host arrays) --------------------------- */
+
+/* Tree construction + neighbour search for every particle
+ * (replaces clumping_tree_main.cpp:390-395 and :418-430 around
+ * KDTree::construct, kdtree_balanced.h:17, and neighbor_search,
+ * nbr_search.h:9).  Sets p[i].rk = sqrtf(d2 of the 33rd nearest, self
+ * included) and adds to p[i].dens the tent weights of every query that has i
+ * among its 32 nearest.  Neighbours are the 33 smallest keys (d2, index).
+ * [left, right) is the buffered cube (-b*L, (1+b)*L). */
+int asg_neighbor_search(asg_ctx* ctx, asg_particle* p, int np, float left, float right);
+
+/* clear_mesh + assign_on_mesh for one mesh (coarse_mesh.h:4-8, called at
+ * clumping_tree_main.cpp:525-526): mesh gets 6*nc^3 floats in the reference
+ * layout [n | halo | c | v (xyz interleaved)].  totals (optional, 2 doubles):
+ * FP64 sums of the n and halo weights (mesh_total, coarse_mesh.h:5). */
+int asg_assign_on_mesh(asg_ctx* ctx, const asg_particle* p, int np, float boxsize, int nc,
+                       int sign, float* mesh, double* totals);
+
+/* The whole per-nc loop (clumping_tree_main.cpp:521-533) in one call:
+ * meshes[k] receives mesh k (6*ncs[k]^3 floats), totals[2k..2k+1] its FP64
+ * Σn, Σhalo.  periodic=1 is assign_on_global_mesh (global_mesh.cpp:25-28) for
+ * the rank at grid coordinates coords[3] (offset = boxsize*coords). */
+int asg_assign_on_meshes(asg_ctx* ctx, const asg_particle* p, int np, float boxsize,
+                         const int* ncs, int n_nc, int sign, int periodic, const int* coords,
+                         float* const* meshes, double* totals);
+
+/* assign_on_density_mesh (coarse_mesh.h:14-16): n channel only, nc^3 floats. */
+int asg_assign_on_density_mesh(asg_ctx* ctx, const asg_particle* p, int np, float boxsize,
+                               int nc, int sign, float* mesh);
+
+/* write_mesh_separate normalisation (coarse_mesh.cpp:158-171) of a host mesh,
+ * in place: c *= vol/n^2, v /= n, n *= 8, halo *= 8 (vol = powf(L/nc, 3)). */
+int asg_normalise_mesh(asg_ctx* ctx, float* mesh, int nc, float boxsize);
+
+/* group_fof (fof.h:7-9, called at clumping_tree_main.cpp:405): p[i].igrp gets
+ * group labels 1..ngroup (every particle is in a group), numbered in order of
+ * each group's smallest input index.  ll is the internal linking length. */
+int asg_group_fof(asg_ctx* ctx, asg_particle* p, int np, float left, float right, float ll,
+                  int* ngroup);
+
+/* remove_small_groups (fof.h:11-12): groups with >= 20 members -> 1..nhalo in
+ * label order, all others -> 0.  Labels must be in [0, ngrp]. */
+int asg_remove_small_groups(asg_ctx* ctx, asg_particle* p, int np, int ngrp, int* nhalo);
+
+/* The SO-halo loop at clumping_tree_main.cpp:465-485 around
+ * mark_halo_particles (nbr_search.h:11): for every halo whose centre is
+ * strictly inside (left, right)^3, particles with d2 < r*r get igrp = -1;
+ * np_halo = sum of the per-halo counts, m_halo = sum of mass/8. */
+int asg_mark_halo_particles(asg_ctx* ctx, asg_particle* p, int np, const asg_halo* halos,
+                            int nh, float left, float right, long* np_halo, double* m_halo);
+
+/* The per-redshift hot path in one call: tree, neighbour search, SO-halo
+ * marking (nh may be 0), then the deposit for every nc with sign, written to
+ * meshes[k] (host, 6*nc^3 floats each) and totals[2k..2k+1].  p is updated in
+ * place (rk, dens, igrp). */
+int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, float boxsize,
+               const asg_halo* halos, int nh, const int* ncs, int n_nc, int sign,
+               float* const* meshes, double* totals, long* np_halo, double* m_halo);
+
+/* ---- staged device-resident interface --------------------------------------- */
+
+/* Load a particle set and build its index (H2D + sort + tree).  Subsequent
+ * asg_run_* calls work on it until the next load. */
+int asg_load_particles(asg_ctx* ctx, const asg_particle* p, int np, float left, float right);
+/* Same from device arrays: x (np*3), v (np*3, may be NULL), dens (np, may be
+ * NULL = 0), igrp (np, may be NULL = 0). */
+int asg_load_particles_device(asg_ctx* ctx, const float* d_x, const float* d_v,
+                              const float* d_dens, const int* d_igrp, int np, float left,
+                              float right);
+int asg_run_neighbor_search(asg_ctx* ctx);
+int asg_run_mark_halos(asg_ctx* ctx, const asg_halo* halos, int nh, long* np_halo,
+                       double* m_halo);
+int asg_run_fof(asg_ctx* ctx, float ll, int* ngroup);
+int asg_run_remove_small_groups(asg_ctx* ctx, int ngrp, int* nhalo);
+/* Deposit for every nc into library-owned device meshes (read them with
+ * asg_mesh_device or asg_copy_mesh); totals (host, 2 per mesh) optional. */
+int asg_run_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,
+                    int periodic, const int* coords, int density_only, double* totals);
+/* Normalise device mesh k in place (write_mesh_separate semantics). */
+int asg_run_normalise(asg_ctx* ctx, int k);
+/* Device pointer of mesh k from the last asg_run_deposit. */
+float* asg_mesh_device(asg_ctx* ctx, int k);
+int asg_copy_mesh(asg_ctx* ctx, int k, float* host);
+/* Write the loaded set back (input order) as Particle records. */
+int asg_store_particles(asg_ctx* ctx, asg_particle* p);
+/* Input-order fields to device arrays (any may be NULL). */
+int asg_store_fields_device(asg_ctx* ctx, float* d_rk, float* d_dens, int* d_igrp);
+/* Neighbour-search internals in input order (host arrays, any may be NULL):
+ * t33 = d2 of the 33rd key, idx33 = its input index. */
+int asg_get_knn(asg_ctx* ctx, float* t33, int* idx33);
+/* CUDA stream used by the context (cudaStream_t as void*). */
+void* asg_stream(asg_ctx* ctx);
+/* Count of kernels this library has launched so far (process-wide). */
+long long asg_kernel_launches(asg_ctx* ctx);
+
+/* ---- measurement ---------------------------------------------------------------- */
+/* Phase timing with CUDA events on the context stream.  enable != 0 turns it on
+ * and zeroes the accumulators; asg_phase_ms fills ms[0..ASG_NPHASES-1] with the
+ * device time accumulated per phase since then. */
+#define ASG_NPHASES 8
+enum { ASG_PH_INDEX = 0, ASG_PH_KNN = 1, ASG_PH_TIES = 2, ASG_PH_BOXES = 3, ASG_PH_DENS = 4,
+       ASG_PH_DEPOSIT = 5, ASG_PH_HALOS = 6, ASG_PH_FOF = 7 };
+int asg_set_timing(asg_ctx* ctx, int enable);
+int asg_phase_ms(asg_ctx* ctx, double* ms);
+const char* asg_phase_name(int phase);
+/* Measured FP32 FMA throughput of this GPU (TFLOP/s, 2 flops per FMA) from a
+ * register-resident FMA-chain kernel over all SMs: the FP32 roofline ceiling. */
+int asg_measure_fp32_peak(asg_ctx* ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

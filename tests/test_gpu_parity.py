@@ -1,0 +1,259 @@
+"""GPU parity tests: the CUDA path through the C ABI against the reference's own
+outputs (golden fixtures) and the CPU oracle.
+
+Bars: bit-exact rk, neighbour sets (the 33 smallest keys (d2, index)), SO-halo
+marks, FOF membership and normalisation; fields within the stated tolerance of
+the FP64 oracle (per-cell relative error <= 1e-5 for cells above 1e-3 of the
+mean); FP64 mass totals within 1e-10 of the oracle's FP64 sum of the same
+float weights."""
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle as po
+from helpers import exact_t33, rel_err_cells, set_from_key
+
+from asmooth_gb300 import api
+from asmooth_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-5  # per-cell relative error vs FP64, cells above 1e-3 of the mean
+MASS_TOL = 1e-10  # FP64 total of the deposited float weights
+NTHREADS = os.cpu_count() or 1
+
+
+def bits(a):
+    return np.asarray(a, np.float32).view(np.int32)
+
+
+def halos_of(rows):
+    rows = np.asarray(rows, np.float32).reshape(-1, 5)
+    return api.make_halos(rows[:, :3], rows[:, 3], rows[:, 4])
+
+
+def check_mesh(mesh, m64, nc, tol=FIELD_TOL):
+    nm = nc ** 3
+    n64, h64, c64, v64 = m64[:nm], m64[nm:2 * nm], m64[2 * nm:3 * nm], m64[3 * nm:]
+    n, h, c, v = mesh[:nm], mesh[nm:2 * nm], mesh[2 * nm:3 * nm], mesh[3 * nm:]
+    assert rel_err_cells(n, n64, n64) <= tol
+    assert rel_err_cells(c, c64, n64) <= tol
+    if h64.max() > 0:
+        assert rel_err_cells(h, h64, h64) <= tol
+    scale = np.abs(v64) + np.repeat(n64, 3)
+    assert np.all(np.abs(v.astype(np.float64) - v64) <= tol * scale + 1e-30)
+
+
+# ---- golden fixtures (the reference's own outputs) -----------------------------------
+
+def test_neighbor_search_golden(gpu_ctx, golden, oracle):
+    g = golden
+    x = g["x"]
+    p = api.make_particles(x, g["v"])
+    gpu_ctx.neighbor_search(p, g["left"], g["right"])
+    assert np.array_equal(bits(p["rk"]), bits(g["rk"]))
+    assert np.array_equal(p["x"], x) and np.array_equal(p["v"], g["v"])  # order preserved
+    t33, idx33 = gpu_ctx.get_knn(len(x))
+    for q, ref in zip(g["nbr_sample"], g["nbr"]):
+        assert np.array_equal(set_from_key(x, int(q), t33[q], idx33[q]), ref)
+    # dens: reference float sums in kd-tree order vs our fixed-order double-float sums
+    assert np.max(np.abs(p["dens"] - g["dens"]) / g["dens"]) <= FIELD_TOL
+    te, ie, nbr = oracle.knn_exact(x, g["left"], g["right"], NTHREADS)
+    assert np.array_equal(bits(te), bits(t33)) and np.array_equal(ie, idx33)
+    _, _, d64 = oracle.dens_from_lists(x, nbr, te)
+    assert np.max(np.abs(p["dens"] - d64) / d64) <= FIELD_TOL
+
+
+def test_mark_halos_golden(gpu_ctx, golden):
+    g = golden
+    p = api.make_particles(g["x"], g["v"])
+    nph, mh = gpu_ctx.mark_halo_particles(p, halos_of(g["halos"]), g["left"], g["right"])
+    assert np.array_equal(p["igrp"], g["igrp_marked"])
+    assert nph == g["np_halo"] and mh == g["m_halo"]
+
+
+def test_mesh_golden(gpu_ctx, golden, oracle):
+    g = golden
+    ncs = [int(nc) for nc in g["ncs"]]
+    p = api.make_particles(g["x"], g["v"], dens=g["dens"], rk=g["rk"], igrp=g["igrp_marked"])
+    meshes, tot = gpu_ctx.assign_on_meshes(p, g["boxsize"], ncs, sign=-1)
+    for k, nc in enumerate(ncs):
+        ref = g[f"mesh{nc}"]
+        _, m64, t64 = oracle.assign_on_mesh(g["x"], g["v"], g["dens"], g["rk"], g["igrp_marked"],
+                                            g["boxsize"], nc, -1)
+        check_mesh(meshes[k], m64, nc)
+        nm = nc ** 3
+        assert rel_err_cells(meshes[k][:nm], ref[:nm], ref[:nm]) <= FIELD_TOL
+        assert abs(tot[k, 0] - t64[0]) <= MASS_TOL * t64[0]
+        assert abs(tot[k, 1] - t64[1]) <= MASS_TOL * max(t64[1], 1.0)
+        # the reference's own mass check on the float mesh
+        assert abs(api.mesh_total(meshes[k], nc) - g[f"total{nc}"][0]) <= 1e-6 * g[f"total{nc}"][0]
+
+
+def test_normalise_golden(gpu_ctx, golden):
+    g = golden
+    for nc in g["ncs"]:
+        out = gpu_ctx.normalise_mesh(g[f"mesh{nc}"], int(nc), g["boxsize"])
+        assert np.array_equal(bits(out), bits(g[f"norm{nc}"]))
+
+
+def test_global_and_density_mesh_golden(gpu_ctx, golden, oracle):
+    g = golden
+    nc = int(g["ncs"][0])
+    L = float(g["boxsize"])
+    p = api.make_particles(g["x"], g["v"], dens=g["dens"], rk=g["rk"], igrp=g["igrp_marked"])
+    mg, tg = gpu_ctx.assign_on_global_mesh(p, L, nc, -1, coords=(1, 0, 2))
+    _, m64, t64 = oracle.assign_on_mesh(g["x"], g["v"], g["dens"], g["rk"], g["igrp_marked"], L, nc,
+                                        -1, periodic=True, offset=(L, 0.0, 2 * L))
+    check_mesh(mg, m64, nc)
+    ref = g[f"global{nc}"]
+    assert rel_err_cells(mg[: nc ** 3], ref[: nc ** 3], ref[: nc ** 3]) <= FIELD_TOL
+    assert abs(tg[0] - t64[0]) <= MASS_TOL * t64[0]
+    md = gpu_ctx.assign_on_density_mesh(p, L, nc, -1)
+    ref = g[f"density{nc}"]
+    assert rel_err_cells(md, ref, ref) <= FIELD_TOL
+
+
+def test_fof_golden(gpu_ctx, golden):
+    g = golden
+    p = api.make_particles(g["x"], g["v"])
+    ng = gpu_ctx.group_fof(p, g["left"], g["right"], g["ll"])
+    assert ng == g["ngroup"]
+    lab = p["igrp"].copy()
+    assert np.array_equal(po.canonical_groups(lab), g["fof"])
+    # labels 1..ng numbered by each group's smallest input index
+    first = np.full(ng + 1, -1)
+    for i in range(len(lab) - 1, -1, -1):
+        first[lab[i]] = i
+    assert lab.min() == 1 and lab.max() == ng and np.all(np.diff(first[1:]) > 0)
+    nh = gpu_ctx.remove_small_groups(p, ng)
+    assert nh == g["nhalo"]
+    assert np.array_equal(po.canonical_groups(p["igrp"]), g["fof_halo"])
+
+
+# ---- larger seeded cubes against the oracle -------------------------------------------
+
+@pytest.mark.parametrize("name,scale", [("cfg1", 1), ("cfg2", 4)])
+def test_cube_vs_oracle(gpu_ctx, oracle, name, scale):
+    cube, ncs = syn.make_workload(name, scale=scale)
+    x = cube.x
+    p = api.make_particles(x, cube.v)
+    gpu_ctx.neighbor_search(p, cube.left, cube.right)
+    t33, idx33 = gpu_ctx.get_knn(cube.n)
+    te, ie, nbr = oracle.knn_exact(x, cube.left, cube.right, NTHREADS)
+    assert np.array_equal(bits(t33), bits(te)) and np.array_equal(idx33, ie)
+    # the reference's own traversal rule (faithful port) gives the same rk
+    rk_ref, dens_ref = oracle.neighbor_search(x, cube.left, cube.right)
+    assert np.array_equal(bits(p["rk"]), bits(rk_ref))
+    _, _, d64 = oracle.dens_from_lists(x, nbr, te)
+    assert np.max(np.abs(p["dens"] - d64) / d64) <= FIELD_TOL
+    assert np.max(np.abs(p["dens"] - dens_ref) / dens_ref) <= FIELD_TOL
+    meshes, tot = gpu_ctx.assign_on_meshes(p, cube.boxsize, ncs, sign=-1)
+    for k, nc in enumerate(ncs):
+        _, m64, t64 = oracle.assign_on_mesh(x, cube.v, p["dens"], p["rk"], p["igrp"], cube.boxsize,
+                                            nc, -1)
+        check_mesh(meshes[k], m64, nc)
+        assert abs(tot[k, 0] - t64[0]) <= MASS_TOL * t64[0]
+        assert 0.999 < tot[k].sum() / cube.n_local < 1.001
+
+
+def test_fof_cube_vs_oracle(gpu_ctx, oracle):
+    cube, _ = syn.make_workload("cfg2", scale=4)
+    p = api.make_particles(cube.x, cube.v)
+    ll = np.float32(0.4)
+    ng = gpu_ctx.group_fof(p, cube.left, cube.right, ll)
+    lab, ng_ref = oracle.group_fof(cube.x, cube.left, cube.right, ll, exact=True)
+    assert ng == ng_ref
+    assert np.array_equal(po.canonical_groups(p["igrp"]), po.canonical_groups(lab))
+
+
+def test_smooth_pipeline_matches_staged_calls(gpu_ctx):
+    cube, ncs = syn.make_workload("cfg1", scale=2)
+    rng = np.random.default_rng(5)
+    nh = 40
+    halos = api.make_halos(cube.x[rng.choice(cube.n_local, nh)], rng.uniform(0.5, 3, nh),
+                           rng.uniform(10, 1000, nh))
+    p1 = api.make_particles(cube.x, cube.v)
+    m1, t1, nph1, mh1 = gpu_ctx.smooth(p1, cube.left, cube.right, cube.boxsize, ncs, -1, halos)
+    p2 = api.make_particles(cube.x, cube.v)
+    gpu_ctx.neighbor_search(p2, cube.left, cube.right)
+    nph2, mh2 = gpu_ctx.mark_halo_particles(p2, halos, cube.left, cube.right)
+    m2, t2 = gpu_ctx.assign_on_meshes(p2, cube.boxsize, ncs, sign=-1)
+    assert nph1 == nph2 and mh1 == mh2
+    assert p1.tobytes() == p2.tobytes()
+    for a, b in zip(m1, m2):
+        assert np.array_equal(bits(a), bits(b))
+    assert np.array_equal(t1, t2)
+
+
+def test_full_size_cfg2_properties(gpu_ctx):
+    """256^3 particles, side 512: determinism, exactness of sampled queries
+    against brute force, the reference's mass check."""
+    cube, ncs = syn.make_workload("cfg2")
+    x = cube.x
+    p = api.make_particles(x, cube.v)
+    meshes1, tot1, _, _ = gpu_ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1)
+    t33, idx33 = gpu_ctx.get_knn(cube.n)
+    p2 = api.make_particles(x, cube.v)
+    meshes2, tot2, _, _ = gpu_ctx.smooth(p2, cube.left, cube.right, cube.boxsize, ncs, -1)
+    assert p.tobytes() == p2.tobytes()
+    for a, b in zip(meshes1, meshes2):
+        assert np.array_equal(bits(a), bits(b))
+    assert np.array_equal(tot1, tot2)
+    rng = np.random.default_rng(7)
+    for q in rng.choice(cube.n, 64, replace=False):
+        t, k = exact_t33(x, int(q))
+        assert t == t33[q] and k == idx33[q]
+        assert p["rk"][q] == np.sqrt(np.float32(t))
+    for k, nc in enumerate(ncs):
+        assert 0.999 < tot1[k].sum() / cube.n_local < 1.001
+
+
+# ---- edge cases --------------------------------------------------------------------
+
+def test_errors_are_reported_not_faulted(gpu_ctx):
+    x = np.random.default_rng(1).uniform(0, 10, (20, 3)).astype(np.float32)
+    with pytest.raises(api.AsmoothError) as e:
+        gpu_ctx.neighbor_search(api.make_particles(x), 0.0, 10.0)
+    assert e.value.status == api.ASG_ERR_FEW
+    x = np.random.default_rng(2).uniform(0, 10, (100, 3)).astype(np.float32)
+    x[5, 1] = np.nan
+    with pytest.raises(api.AsmoothError) as e:
+        gpu_ctx.neighbor_search(api.make_particles(x), 0.0, 10.0)
+    assert e.value.status == api.ASG_ERR_NONFINITE
+    x = np.random.default_rng(3).uniform(0, 10, (100, 3)).astype(np.float32)
+    x[:40] = x[0]
+    with pytest.raises(api.AsmoothError) as e:
+        gpu_ctx.neighbor_search(api.make_particles(x), 0.0, 10.0)
+    assert e.value.status == api.ASG_ERR_ZERO_RK
+    p = api.make_particles(np.random.default_rng(4).uniform(0, 10, (100, 3)), rk=np.ones(100))
+    with pytest.raises(api.AsmoothError) as e:
+        gpu_ctx.assign_on_meshes(p, 10.0, [0])
+    assert e.value.status == api.ASG_ERR_ARG
+    with pytest.raises(api.AsmoothError):
+        gpu_ctx.neighbor_search(api.make_particles(np.zeros((100, 3))), 1.0, 0.0)
+    # the context stays usable after errors
+    x = np.random.default_rng(5).uniform(0, 10, (500, 3)).astype(np.float32)
+    gpu_ctx.neighbor_search(api.make_particles(x), 0.0, 10.0)
+
+
+def test_lattice_ties_by_index(gpu_ctx, oracle):
+    g = np.arange(10, dtype=np.float32)
+    X = (np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3) + 0.5).astype(np.float32)
+    p = api.make_particles(X)
+    gpu_ctx.neighbor_search(p, 0.0, 10.0)
+    t33, idx33 = gpu_ctx.get_knn(len(X))
+    te, ie, nbr = oracle.knn_exact(X, 0.0, 10.0, NTHREADS)
+    assert np.array_equal(bits(t33), bits(te)) and np.array_equal(idx33, ie)
+    _, _, d64 = oracle.dens_from_lists(X, nbr, te)
+    assert np.max(np.abs(p["dens"] - d64) / d64) <= FIELD_TOL
+
+
+def test_empty_halo_list_and_small_sets(gpu_ctx):
+    x = np.random.default_rng(9).uniform(0, 10, (33, 3)).astype(np.float32)
+    p = api.make_particles(x)
+    gpu_ctx.neighbor_search(p, 0.0, 10.0)  # exactly 33 particles: rk = farthest
+    d2max = max(float(((x - x[i]) ** 2).sum(1).max()) for i in range(1))
+    assert abs(p["rk"][0] ** 2 - d2max) <= 1e-5 * d2max
+    assert gpu_ctx.mark_halo_particles(p, api.make_halos(np.zeros((0, 3)), [], []), 0.0, 10.0) == (0, 0.0)

@@ -1,0 +1,184 @@
+"""CPU tests of the oracle: pinned to the reference's own outputs (golden
+fixtures generated from the reference by tests/golden/make_golden.py) and to
+known-answer cases.  No GPU is used."""
+import numpy as np
+import pytest
+
+import pyoracle as po
+from helpers import d2_to_all, exact_t33
+
+from asmooth_gb300 import synthetic as syn
+
+
+def bits(a):
+    return np.asarray(a, np.float32).view(np.int32)
+
+
+# ---- faithful restatement == reference (golden) --------------------------------
+
+def test_neighbor_search_matches_reference(oracle, golden):
+    g = golden
+    rk, dens, nbr, _ = oracle.neighbor_search(g["x"], g["left"], g["right"], want_nbr=True)
+    assert np.array_equal(bits(rk), bits(g["rk"]))
+    assert np.array_equal(bits(dens), bits(g["dens"]))
+    assert np.array_equal(np.sort(nbr[g["nbr_sample"]], axis=1), g["nbr"])
+
+
+def test_exact_knn_definition_matches_reference(oracle, golden):
+    """The order-independent definition the GPU implements (top-33 by
+    (d2, index)) selects the same sets and rk as the reference here."""
+    g = golden
+    t33, idx33, nbr = oracle.knn_exact(g["x"], g["left"], g["right"])
+    assert np.array_equal(bits(np.sqrt(t33)), bits(g["rk"]))
+    assert np.array_equal(np.sort(nbr[g["nbr_sample"]], axis=1), g["nbr"])
+    # spot-check the exact oracle against brute force
+    for q in g["nbr_sample"][:20]:
+        t, k = exact_t33(g["x"], int(q))
+        assert t == t33[q] and k == idx33[q]
+
+
+def test_mark_halos_matches_reference(oracle, golden):
+    g = golden
+    igrp, nph, mh = oracle.mark_halo_particles(g["x"], g["left"], g["right"], g["halos"])
+    assert np.array_equal(igrp, g["igrp_marked"])
+    assert nph == g["np_halo"] and mh == g["m_halo"]
+
+
+def test_mesh_matches_reference(oracle, golden):
+    g = golden
+    for nc in g["ncs"]:
+        mesh, m64, tot = oracle.assign_on_mesh(g["x"], g["v"], g["dens"], g["rk"], g["igrp_marked"],
+                                               g["boxsize"], int(nc), -1)
+        assert np.array_equal(bits(mesh), bits(g[f"mesh{nc}"]))
+        assert oracle.mesh_total(mesh, int(nc)) == g[f"total{nc}"][0]
+        # FP64 totals of the float weights agree with the float mesh to float rounding
+        assert abs(tot[0] - g[f"total{nc}"][0]) <= 1e-6 * tot[0]
+        norm = oracle.normalise_mesh(mesh, int(nc), g["boxsize"])
+        assert np.array_equal(bits(norm), bits(g[f"norm{nc}"]))
+
+
+def test_global_and_density_mesh_match_reference(oracle, golden):
+    g = golden
+    nc = int(g["ncs"][0])
+    L = float(g["boxsize"])
+    mg, _, _ = oracle.assign_on_mesh(g["x"], g["v"], g["dens"], g["rk"], g["igrp_marked"], L, nc, -1,
+                                     periodic=True, offset=(L, 0.0, 2 * L), want64=False)
+    assert np.array_equal(bits(mg), bits(g[f"global{nc}"]))
+    md = oracle.assign_on_density_mesh(g["x"], g["rk"], g["igrp_marked"], L, nc, -1)
+    assert np.array_equal(bits(md), bits(g[f"density{nc}"]))
+
+
+def test_fof_matches_reference(oracle, golden):
+    g = golden
+    lab, ng = oracle.group_fof(g["x"], g["left"], g["right"], g["ll"])
+    assert ng == g["ngroup"]
+    assert np.array_equal(po.canonical_groups(lab), g["fof"])
+    lab_e, ng_e = oracle.group_fof(g["x"], g["left"], g["right"], g["ll"], exact=True)
+    assert ng_e == g["ngroup"]
+    assert np.array_equal(po.canonical_groups(lab_e), g["fof"])
+    h, nh = oracle.remove_small_groups(lab, ng)
+    assert nh == g["nhalo"]
+    assert np.array_equal(po.canonical_groups(h), g["fof_halo"])
+
+
+# ---- known answers -----------------------------------------------------------------
+
+def test_single_particle_mass_is_one(oracle):
+    """ker_integ integrates the unit tent exactly: an unclipped particle deposits 1."""
+    x = np.array([[10.3, 11.7, 12.05]], np.float32)
+    for h in (0.3, 1.0, 2.7, 5.0):
+        for nc in (8, 32):
+            mesh, m64, tot = oracle.assign_on_mesh(x, np.zeros((1, 3), np.float32),
+                                                   np.ones(1, np.float32), np.array([h], np.float32),
+                                                   np.zeros(1, np.int32), 32.0, nc, -1)
+            assert abs(tot[0] - 1.0) < 2e-6
+            assert abs(m64[: nc ** 3].sum() - 1.0) < 1e-12
+            assert tot[1] == 0.0
+
+
+def test_sign_selects_halo_channel(oracle):
+    x = np.array([[8.0, 8.0, 8.0], [20.0, 20.0, 20.0]], np.float32)
+    rk = np.array([1.0, 1.0], np.float32)
+    v = np.ones((2, 3), np.float32)
+    d = np.ones(2, np.float32)
+    ig = np.array([-1, 3], np.int32)
+    nc = 16
+    for sign, halo_of in ((-1, 0), (1, 1)):
+        mesh, _, tot = oracle.assign_on_mesh(x, v, d, rk, ig, 32.0, nc, sign)
+        # sign*igrp > 0 goes to the halo channel (coarse_mesh.cpp:95-122)
+        assert abs(tot[1] - 1.0) < 2e-6 and abs(tot[0] - 1.0) < 2e-6
+        nm = nc ** 3
+        halo = mesh[nm:2 * nm].reshape(nc, nc, nc)
+        cell = (x[halo_of] / 2).astype(int)
+        assert halo[cell[2] - 1:cell[2] + 1, cell[1] - 1:cell[1] + 1, cell[0] - 1:cell[0] + 1].sum() > 0.99
+
+
+def test_cubic_lattice_rk_and_ties(oracle):
+    """Simple cubic lattice with spacing 1: the 33 nearest of an interior point
+    are self + 6 + 12 + 8 + 6 (d2 = 0,1,2,3,4), so rk = 2 and the 33rd key is
+    the largest index among the 6 ties at d2 = 4."""
+    g = np.arange(9, dtype=np.float32)
+    X = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3) + 0.5
+    t33, idx33, nbr = oracle.knn_exact(X, 0.0, 9.0)
+    centre = int(np.argmin(np.abs(X - 4.5).sum(1)))
+    assert t33[centre] == 4.0
+    ties = np.nonzero(d2_to_all(X, X[centre]) == 4.0)[0]
+    assert ties.size == 6 and idx33[centre] == ties.max()
+    rk, d32, d64 = oracle.dens_from_lists(X, nbr, t33)
+    assert rk[centre] == 2.0
+    # centre receives from itself (1/8) and from its neighbours whose sets contain it
+    assert d64[centre] > 0.125
+
+
+def test_fof_link_is_inclusive(oracle):
+    """Friends at exactly ll are linked (d2 <= ll*ll, fof.cpp:86)."""
+    ll = np.float32(0.5)
+    x = np.array([[1.0, 1.0, 1.0], [1.5, 1.0, 1.0], [2.0, 1.0, 1.0], [2.75, 1.0, 1.0]], np.float32)
+    lab, ng = oracle.group_fof(x, 0.0, 4.0, ll)
+    assert ng == 2 and lab[0] == lab[1] == lab[2] != lab[3]
+
+
+def test_mass_totals_with_shell(oracle):
+    """With the periodic shell the deposited mass exceeds N only by the shell
+    particles' kernel tails inside the cube: the reference's 0.1% check."""
+    cube, ncs = syn.make_workload("cfg1", scale=4)
+    rk, dens = oracle.neighbor_search(cube.x, cube.left, cube.right)
+    ig = np.zeros(cube.n, np.int32)
+    for nc in ncs:
+        _, _, tot = oracle.assign_on_mesh(cube.x, cube.v, dens, rk, ig, cube.boxsize, nc, -1)
+        assert 0.999 < tot.sum() / cube.n_local < 1.001
+
+
+def test_synthetic_is_seeded_and_shell_is_periodic():
+    a, _ = syn.make_workload("cfg1", scale=8)
+    b, _ = syn.make_workload("cfg1", scale=8)
+    assert np.array_equal(a.x, b.x) and a.n_local == b.n_local
+    x = a.x[: a.n_local]
+    assert x.min() >= 0 and x.max() < a.boxsize
+    sh = a.x[a.n_local:]
+    assert np.all((sh > a.left) & (sh < a.right))
+    # every shell copy is an interior particle shifted by a multiple of L (float add)
+    L = np.float32(a.boxsize)
+    shifted = set()
+    for s in np.array(np.meshgrid([-L, 0, L], [-L, 0, L], [-L, 0, L])).T.reshape(-1, 3):
+        shifted.update(map(tuple, (x + s.astype(np.float32)).astype(np.float32).tolist()))
+    assert all(tuple(y.tolist()) in shifted for y in sh)
+
+
+def test_xv_roundtrip(tmp_path):
+    x, v = syn.uniform_cube(1000, 16.0, 3)
+    p = tmp_path / "0.000xv0.dat"
+    syn.write_xv(str(p), x, v)
+    assert p.stat().st_size == 48 + 24 * 1000
+    x2, v2 = syn.read_xv(str(p))
+    assert np.array_equal(x, x2) and np.array_equal(v, v2)
+
+
+@pytest.mark.skipif(not po.Reference.available(), reason="reference not built here")
+def test_oracle_matches_reference_on_clustered_cube(oracle):
+    """Direct reference run (where the reference sources are present)."""
+    R = po.Reference()
+    cube, _ = syn.make_workload("cfg2", scale=8)
+    rk_r, d_r = R.neighbor_search(cube.x, cube.left, cube.right)
+    rk_o, d_o = oracle.neighbor_search(cube.x, cube.left, cube.right)
+    assert np.array_equal(bits(rk_r), bits(rk_o)) and np.array_equal(bits(d_r), bits(d_o))
