@@ -57,6 +57,8 @@ struct asg_ctx {
     Buf uf, minin, mark, scan_tmp, lab_cnt, lab_scan;
     Buf halos, hcount, hmass;
     Buf totals, lohi;
+    Buf dep_lists, dep_counter, dep_ranges, dep_partial;
+    uint32_t* h_u32 = nullptr;  // pinned
     float mesh_boxsize = 0.0f;
     std::vector<MeshBuf> meshes;
 
@@ -297,6 +299,7 @@ int asg_create(asg_ctx** out, int device)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_u32, 4 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->s);
     if (e != cudaSuccess) {
@@ -319,7 +322,8 @@ void asg_destroy(asg_ctx* ctx)
                    &ctx->meta, &ctx->parent, &ctx->leaf_parent, &ctx->flags, &ctx->blo,
                    &ctx->bhi, &ctx->elo, &ctx->ehi, &ctx->uf, &ctx->minin, &ctx->mark,
                    &ctx->scan_tmp, &ctx->lab_cnt, &ctx->lab_scan, &ctx->halos, &ctx->hcount,
-                   &ctx->hmass, &ctx->totals, &ctx->lohi};
+                   &ctx->hmass, &ctx->totals, &ctx->lohi, &ctx->dep_lists, &ctx->dep_counter,
+                   &ctx->dep_ranges, &ctx->dep_partial};
     for (Buf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& m : ctx->meshes) {
@@ -329,6 +333,7 @@ void asg_destroy(asg_ctx* ctx)
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->h_u32) cudaFreeHost(ctx->h_u32);
     if (ctx->s) cudaStreamDestroy(ctx->s);
     delete ctx;
 }
@@ -569,9 +574,30 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
         tiles += tpd * tpd * tpd;
     }
     if (int r = grow(ctx, ctx->totals, 16 * (size_t)n_nc)) return r;
+    // per-tile candidate lists: count, then size the lists and the work items
+    const size_t T1 = (size_t)tiles + 1;
+    if (int r = grow(ctx, ctx->dep_lists, deposit_list_temp_bytes(tiles))) return r;
+    if (int r = grow(ctx, ctx->dep_counter, 16)) return r;
+    DepositScratch w;
+    w.nranges = P<uint32_t>(ctx->dep_lists);
+    w.nparts = w.nranges + T1;
+    w.range_off = w.nparts + T1;
+    w.item_off = w.range_off + T1;
+    w.scan_tmp = (void*)(w.item_off + T1);
+    w.next_item = P<int>(ctx->dep_counter);
     phase_begin(ctx, ASG_PH_DEPOSIT);
-    launch_deposit(P<float4>(ctx->pos), P<float4>(ctx->vel), P<int>(ctx->igrp), P<float>(ctx->rk),
-                   tree_view(ctx), p, tiles, ctx->d_err, ctx->s);
+    launch_deposit_count(P<float4>(ctx->pos), P<float>(ctx->rk), tree_view(ctx), p, tiles, w,
+                         ctx->d_err, ctx->s);
+    CK(cudaMemcpyAsync(ctx->h_u32, w.range_off + tiles, 4, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(ctx->h_u32 + 1, w.item_off + tiles, 4, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    const uint32_t nranges = ctx->h_u32[0], nitems = ctx->h_u32[1];
+    if (int r = grow(ctx, ctx->dep_ranges, 16 * (size_t)nranges + 16)) return r;
+    if (int r = grow(ctx, ctx->dep_partial, deposit_partial_bytes(nitems) + 16)) return r;
+    w.ranges = P<int4>(ctx->dep_ranges);
+    w.partial = P<float>(ctx->dep_partial);
+    launch_deposit_run(P<float4>(ctx->pos), P<float4>(ctx->vel), P<int>(ctx->igrp),
+                       P<float>(ctx->rk), tree_view(ctx), p, tiles, w, ctx->d_err, ctx->s);
     for (int k = 0; k < n_nc; ++k) {
         const int tpd = (ncs[k] + 7) / 8;
         launch_reduce_partials(P<double>(ctx->meshes[(size_t)k].partial), tpd * tpd * tpd,

@@ -95,9 +95,27 @@ struct DepositParams {
     float offset[3];  // periodic: rank cube offset
     int density_only;
 };
-void launch_deposit(const float4* pos, const float4* vel, const int* igrp, const float* rk,
-                    const TreeView& t, const DepositParams& p, int total_tiles, int* err,
-                    cudaStream_t s);
+// scratch of one deposit: per-tile candidate lists and work items
+struct DepositScratch {
+    uint32_t* nranges;    // [T] bucket ranges listed per tile
+    uint32_t* nparts;     // [T] candidate particles per tile
+    uint32_t* range_off;  // [T+1] exclusive scan of nranges
+    uint32_t* item_off;   // [T+1] exclusive scan of work items per tile
+    void* scan_tmp;       // scan scratch for T+1 entries
+    int4* ranges;         // [range_off[T]] first, last, flattened start, -
+    float* partial;       // [item_off[T]] partial tiles of multi-segment tiles
+    int* next_item;       // work counter of the persistent kernel
+};
+size_t deposit_list_temp_bytes(int total_tiles);
+size_t deposit_partial_bytes(uint32_t items);
+// pass 1: count candidates per tile, scan offsets (range_off[T], item_off[T] hold the totals)
+int launch_deposit_count(const float4* pos, const float* rk, const TreeView& t,
+                         const DepositParams& p, int total_tiles, DepositScratch& w, int* err,
+                         cudaStream_t s);
+// pass 2: fill the lists, deposit every (tile, segment), merge multi-segment tiles
+void launch_deposit_run(const float4* pos, const float4* vel, const int* igrp, const float* rk,
+                        const TreeView& t, const DepositParams& p, int total_tiles,
+                        DepositScratch& w, int* err, cudaStream_t s);
 void launch_reduce_partials(const double* partial, int ntiles, double* out2, cudaStream_t s);
 void launch_normalise(float* mesh, int nc, float vol, cudaStream_t s);
 

@@ -193,7 +193,8 @@ def run_ours(args):
     from asmooth_gb300 import synthetic as syn
 
     seed = 2 + 1000 * rank  # independent replica cube per rank
-    cube, ncs = syn.make_workload(WORKLOAD, seed=seed)
+    scale = 2 if args.workload == "cfg2_s2" else 1
+    cube, ncs = syn.make_workload(WORKLOAD, seed=seed, scale=scale)
     n, n_local = cube.n, cube.n_local
     x_d = torch.from_numpy(cube.x).cuda()
     v_d = torch.from_numpy(cube.v).cuda()
@@ -244,30 +245,38 @@ def run_ours(args):
 
     # end to end through the public C ABI: pinned host Particle records in, out
     rec_bytes = n * api.PARTICLE_DTYPE.itemsize
-    host = torch.empty(rec_bytes, dtype=torch.uint8, pin_memory=True)
-    p = host.numpy().view(api.PARTICLE_DTYPE)
-    p[:] = api.make_particles(cube.x, cube.v)
-    mesh_host = [torch.empty(6 * nc ** 3, dtype=torch.float32, pin_memory=True).numpy() for nc in ncs]
-    for _ in range(max(1, args.warmup)):
-        ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
-    e2e_times = []
-    for _ in range(args.steps):
-        p["dens"] = 0.0
-        torch.cuda.synchronize()
-        w0 = time.perf_counter()
-        ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
-        e2e_times.append(time.perf_counter() - w0)
-    e2e_s = statistics.mean(e2e_times)
-    tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    e2e_value = world * n_local / float(tt.item())
     d2h = rec_bytes + sum(4 * 6 * nc ** 3 for nc in ncs) + 16 * len(ncs)
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty(rec_bytes, dtype=torch.uint8, pin_memory=True)
+        p = host.numpy().view(api.PARTICLE_DTYPE)
+        p[:] = api.make_particles(cube.x, cube.v)
+        mesh_host = [torch.empty(6 * nc ** 3, dtype=torch.float32, pin_memory=True).numpy()
+                     for nc in ncs]
+        for _ in range(max(1, args.warmup)):
+            ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
+        e2e_times = []
+        for _ in range(args.steps):
+            p["dens"] = 0.0
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
+            e2e_times.append(time.perf_counter() - w0)
+        tt = torch.tensor([statistics.mean(e2e_times)], dtype=torch.float64, device="cuda")
+        if dist:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e = {"value": world * n_local / float(tt.item()), "unit": "particles/s",
+               "h2d_bytes_per_step": rec_bytes, "d2h_bytes_per_step": d2h}
+        rk_host = p["rk"].copy()
+    else:
+        rk_d = torch.empty(n, dtype=torch.float32, device="cuda")
+        ctx.store_fields_device(rk_ptr=rk_d.data_ptr())
+        rk_host = rk_d.cpu().numpy()
 
     # roofline of the dominant kernel (measured live above)
     fp32 = ctx.measure_fp32_peak()
     pk, pk_kind = peaks()
-    cells = deposit_cells(cube.x, p["rk"], cube.boxsize, ncs)
+    cells = deposit_cells(cube.x, rk_host, cube.boxsize, ncs)
     alg = {  # algorithmic FP32 flops per step, per phase
         "knn_t33": 8.0 * 33 * 6 / np.pi * n,  # 8 flops per distance, ~63 candidates per query
         "dens": 14.0 * 32 * n,                 # 14 flops per tent weight, 32 receivers per query
@@ -313,8 +322,7 @@ def run_ours(args):
                                "shell, k=32, nc=64,128,256, plain FP32 form",
                    "n_with_shell": n, "n_local": n_local, "parallelism": f"replicas x{world}",
                    "l2": "flushed before every timed step; inputs larger than L2"},
-        "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": rec_bytes,
-                "d2h_bytes_per_step": d2h},
+        "e2e": e2e,
         "gpu_launches": launches,
         "roofline": roof,
         "clocks": clk,
@@ -337,6 +345,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg2_s2"],
+                    help="cfg2_s2: the same model at 1/8 volume, for profiling captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

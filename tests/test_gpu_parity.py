@@ -34,13 +34,17 @@ def halos_of(rows):
 
 
 def check_mesh(mesh, m64, nc, tol=FIELD_TOL):
+    """Per-cell relative error vs FP64 for cells above 1e-3 of the mean density
+    (the mean of all particles' density, n + halo, over the mesh)."""
     nm = nc ** 3
     n64, h64, c64, v64 = m64[:nm], m64[nm:2 * nm], m64[2 * nm:3 * nm], m64[3 * nm:]
     n, h, c, v = mesh[:nm], mesh[nm:2 * nm], mesh[2 * nm:3 * nm], mesh[3 * nm:]
-    assert rel_err_cells(n, n64, n64) <= tol
-    assert rel_err_cells(c, c64, n64) <= tol
-    if h64.max() > 0:
-        assert rel_err_cells(h, h64, h64) <= tol
+    cut = 1e-3 * float((n64 + h64).mean())
+    for got, ref, dens in ((n, n64, n64), (c, c64, n64), (h, h64, h64)):
+        sel = dens > cut
+        if sel.any():
+            err = np.abs(got[sel].astype(np.float64) - ref[sel]) / np.abs(ref[sel])
+            assert err.max() <= tol
     scale = np.abs(v64) + np.repeat(n64, 3)
     assert np.all(np.abs(v.astype(np.float64) - v64) <= tol * scale + 1e-30)
 
@@ -176,15 +180,30 @@ def test_smooth_pipeline_matches_staged_calls(gpu_ctx):
                            rng.uniform(10, 1000, nh))
     p1 = api.make_particles(cube.x, cube.v)
     m1, t1, nph1, mh1 = gpu_ctx.smooth(p1, cube.left, cube.right, cube.boxsize, ncs, -1, halos)
+    # staged calls on one loaded set: the same index, hence bit-identical results
     p2 = api.make_particles(cube.x, cube.v)
-    gpu_ctx.neighbor_search(p2, cube.left, cube.right)
-    nph2, mh2 = gpu_ctx.mark_halo_particles(p2, halos, cube.left, cube.right)
-    m2, t2 = gpu_ctx.assign_on_meshes(p2, cube.boxsize, ncs, sign=-1)
+    gpu_ctx.load_particles(p2, cube.left, cube.right)
+    gpu_ctx.run_neighbor_search()
+    nph2, mh2 = gpu_ctx.run_mark_halos(halos)
+    t2 = gpu_ctx.run_deposit(cube.boxsize, ncs, sign=-1)
+    m2 = [gpu_ctx.copy_mesh(k, 6 * nc ** 3) for k, nc in enumerate(ncs)]
+    gpu_ctx.store_particles(p2)
     assert nph1 == nph2 and mh1 == mh2
     assert p1.tobytes() == p2.tobytes()
     for a, b in zip(m1, m2):
         assert np.array_equal(bits(a), bits(b))
     assert np.array_equal(t1, t2)
+    # the reference-shaped one-shot calls build their own index (own Morton grid),
+    # so their sums may differ in the last bits only
+    p3 = api.make_particles(cube.x, cube.v)
+    gpu_ctx.neighbor_search(p3, cube.left, cube.right)
+    gpu_ctx.mark_halo_particles(p3, halos, cube.left, cube.right)
+    m3, t3 = gpu_ctx.assign_on_meshes(p3, cube.boxsize, ncs, sign=-1)
+    assert p1.tobytes() == p3.tobytes()
+    for a, b, nc in zip(m1, m3, ncs):
+        n = a[: nc ** 3]
+        assert rel_err_cells(b[: nc ** 3], n.astype(np.float64), n) <= 1e-6
+    assert np.allclose(t1, t3, rtol=1e-12, atol=0)
 
 
 def test_full_size_cfg2_properties(gpu_ctx):
