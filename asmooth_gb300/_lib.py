@@ -48,6 +48,7 @@ SIGNATURES = {
     "asg_phase_ms": (_i, [_vp, _vp]),
     "asg_phase_name": (C.c_char_p, [_i]),
     "asg_measure_fp32_peak": (_i, [_vp, _dp]),
+    "asg_deposit_stats": (_i, [_vp, _vp, _vp, _vp]),
 }
 NPHASES = 8
 

@@ -128,6 +128,11 @@ class Context:
         self._ok(self.lib.asg_phase_ms(self.h, _ptr(ms)))
         return {self.lib.asg_phase_name(i).decode(): float(ms[i]) for i in range(_lib.NPHASES)}
 
+    def deposit_stats(self) -> dict:
+        c, b, i = C.c_longlong(0), C.c_longlong(0), C.c_longlong(0)
+        self._ok(self.lib.asg_deposit_stats(self.h, C.byref(c), C.byref(b), C.byref(i)))
+        return {"candidates": c.value, "buckets": b.value, "items": i.value}
+
     def measure_fp32_peak(self) -> float:
         t = C.c_double(0.0)
         self._ok(self.lib.asg_measure_fp32_peak(self.h, C.byref(t)))

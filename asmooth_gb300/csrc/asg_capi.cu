@@ -842,6 +842,19 @@ __global__ static void k_fma_probe(float* out, int iters, float a, float b)
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+int asg_deposit_stats(asg_ctx* ctx, long long* candidates, long long* buckets, long long* items)
+{
+    if (!ctx) return ASG_ERR_ARG;
+    if (!ctx->dep_counter.p) return fail(ctx, ASG_ERR_STATE, "no deposit run yet");
+    CK(cudaSetDevice(ctx->device));
+    unsigned long long c = 0;
+    CK(cudaMemcpy(&c, P<char>(ctx->dep_counter) + 8, 8, cudaMemcpyDeviceToHost));
+    if (candidates) *candidates = (long long)c;
+    if (buckets) *buckets = ctx->h_u32[0];
+    if (items) *items = ctx->h_u32[1];
+    return ASG_OK;
+}
+
 int asg_measure_fp32_peak(asg_ctx* ctx, double* tflops)
 {
     if (!ctx || !tflops) return ASG_ERR_ARG;

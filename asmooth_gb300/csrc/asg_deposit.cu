@@ -99,15 +99,16 @@ __device__ __forceinline__ bool node_hits_tile(float4 lo, float4 hi, const Depos
 // (1) candidate lists: one warp per tile, depth-first, left subtree first
 // ---------------------------------------------------------------------------
 constexpr int LIST_WARPS = 4;
+constexpr int LIST_STACK = 512;  // per-warp node stack of the lane-parallel walk
 
 template <bool FILL>
 __global__ void __launch_bounds__(LIST_WARPS * 32)
 k_tile_lists(const float4* __restrict__ pos, const float* __restrict__ rk, TreeView t,
              DepositParams P, int total_tiles, uint32_t* __restrict__ nranges,
              uint32_t* __restrict__ nparts, const uint32_t* __restrict__ range_off,
-             int4* __restrict__ ranges, int* err)
+             int4* __restrict__ ranges, int* next_item, int* err)
 {
-    __shared__ int stk[LIST_WARPS][STACK_MAX];
+    __shared__ int stk[LIST_WARPS][LIST_STACK];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x * LIST_WARPS + warp;
     if (tile >= total_tiles) return;
@@ -119,45 +120,69 @@ k_tile_lists(const float4* __restrict__ pos, const float* __restrict__ rk, TreeV
     uint32_t nr = 0, np = 0;
     const uint32_t base = FILL ? range_off[tile] : 0u;
     bool ovf = false;
+    const unsigned lt = lanemask_lt();
     __syncwarp();
-    // lanes test up to 32 stacked nodes at once; hits are expanded in stack order
+    // each round the lanes test up to 32 nodes from the top of the stack; hit
+    // buckets are listed in lane order, hit inner nodes push their children in
+    // lane order (the order depends only on the data: count and fill agree)
     while (sp > 0) {
-        const int node = st[sp - 1];
-        --sp;
+        const int take = (sp + 64 <= LIST_STACK) ? min(sp, 32) : 1;
+        const bool act = lane < take;
+        const int node = act ? st[sp - take + lane] : 0;
+        sp -= take;
         __syncwarp();
-        float4 lo, hi;
-        int first, last;
-        bool bucket;
-        if (node < 0) {
-            const int i = ~node;
-            const float4 p = pos[i];
-            const float h = __fmul_ru(rk[i], 1.000001f);
-            lo = make_float4(__fsub_rd(p.x, h), __fsub_rd(p.y, h), __fsub_rd(p.z, h), 0.f);
-            hi = make_float4(__fadd_ru(p.x, h), __fadd_ru(p.y, h), __fadd_ru(p.z, h), 0.f);
-            first = last = i;
-            bucket = true;
-        } else {
-            const int4 m = t.meta[node];
-            lo = t.elo[node];
-            hi = t.ehi[node];
-            first = m.z;
-            last = m.w;
-            bucket = (m.w - m.z + 1) <= LEAF_MAX;
-        }
-        if (!node_hits_tile(lo, hi, P, ncf, g)) continue;
-        if (bucket) {
-            if (FILL && lane == 0) ranges[base + nr] = make_int4(first, last, (int)np, 0);
-            ++nr;
-            np += (uint32_t)(last - first + 1);
-        } else {
-            if (sp + 2 > STACK_MAX) { ovf = true; break; }
-            const int4 m = t.meta[node];
-            if (lane == 0) {
-                st[sp] = m.y;
-                st[sp + 1] = m.x;
+        bool hit = false, bucket = false;
+        int first = 0, last = -1, c0 = 0, c1 = 0;
+        if (act) {
+            float4 lo, hi;
+            if (node < 0) {
+                const int i = ~node;
+                const float4 p = pos[i];
+                const float h = __fmul_ru(rk[i], 1.000001f);
+                lo = make_float4(__fsub_rd(p.x, h), __fsub_rd(p.y, h), __fsub_rd(p.z, h), 0.f);
+                hi = make_float4(__fadd_ru(p.x, h), __fadd_ru(p.y, h), __fadd_ru(p.z, h), 0.f);
+                first = last = i;
+                bucket = true;
+            } else {
+                const int4 m = t.meta[node];
+                lo = t.elo[node];
+                hi = t.ehi[node];
+                first = m.z;
+                last = m.w;
+                c0 = m.x;
+                c1 = m.y;
+                bucket = (m.w - m.z + 1) <= LEAF_MAX;
             }
-            sp += 2;
+            hit = node_hits_tile(lo, hi, P, ncf, g);
         }
+        const unsigned bmask = __ballot_sync(FULLM, hit && bucket);
+        const unsigned imask = __ballot_sync(FULLM, hit && !bucket);
+        {
+            // exclusive prefix of bucket sizes over lanes (0 for non-buckets)
+            int cnt = (hit && bucket) ? (last - first + 1) : 0;
+            int inc = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULLM, inc, o);
+                if (lane >= o) inc += y;
+            }
+            const int tot = __shfl_sync(FULLM, inc, 31);
+            if (hit && bucket) {
+                const int slot = __popc(bmask & lt);
+                if (FILL) ranges[base + nr + slot] = make_int4(first, last, (int)np + inc - cnt, 0);
+            }
+            nr += __popc(bmask);
+            np += (uint32_t)tot;
+        }
+        const int ni = __popc(imask);
+        if (sp + 2 * ni > LIST_STACK) { ovf = true; break; }
+        if (hit && !bucket) {
+            // the lowest hit lane ends on top: push in reverse lane order
+            const int r = ni - 1 - __popc(imask & lt);
+            st[sp + 2 * r] = c1;
+            st[sp + 2 * r + 1] = c0;
+        }
+        sp += 2 * ni;
         __syncwarp();
     }
     if (lane == 0) {
@@ -165,6 +190,8 @@ k_tile_lists(const float4* __restrict__ pos, const float* __restrict__ rk, TreeV
         if (!FILL) {
             nranges[tile] = nr;
             nparts[tile] = np;
+            // next_item[2..3] accumulate the candidate particle-tile pairs (statistics)
+            atomicAdd(reinterpret_cast<unsigned long long*>(next_item + 2), (unsigned long long)np);
         }
     }
 }
@@ -559,8 +586,9 @@ int launch_deposit_count(const float4* pos, const float* rk, const TreeView& t,
 {
     const int T = total_tiles;
     const int lb = (T + LIST_WARPS - 1) / LIST_WARPS;
+    cudaMemsetAsync(w.next_item, 0, 16, s);
     k_tile_lists<false><<<lb, LIST_WARPS * 32, 0, s>>>(pos, rk, t, p, T, w.nranges, w.nparts,
-                                                       nullptr, nullptr, err);
+                                                       nullptr, nullptr, w.next_item, err);
     // range_off = exclusive scan of nranges; item_off = exclusive scan of items per tile
     cudaMemcpyAsync(w.range_off, w.nranges, 4 * (size_t)T, cudaMemcpyDeviceToDevice, s);
     cudaMemsetAsync(w.range_off + T, 0, 4, s);
@@ -578,7 +606,7 @@ void launch_deposit_run(const float4* pos, const float4* vel, const int* igrp, c
     const int T = total_tiles;
     const int lb = (T + LIST_WARPS - 1) / LIST_WARPS;
     k_tile_lists<true><<<lb, LIST_WARPS * 32, 0, s>>>(pos, rk, t, p, T, nullptr, nullptr,
-                                                      w.range_off, w.ranges, err);
+                                                      w.range_off, w.ranges, nullptr, err);
     cudaMemsetAsync(w.next_item, 0, sizeof(int), s);
     const size_t smem = sizeof(DepShared);
     static bool attr = false;

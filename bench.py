@@ -100,19 +100,23 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def deposit_cells(x, rk, boxsize, ncs):
+def deposit_cells(x, rk, boxsize, ncs, tile=8):
     """Sum over particles and meshes of the cells each deposit touches (the
-    reference's cell-range expression, coarse_mesh.cpp:72-75)."""
+    reference's cell-range expression, coarse_mesh.cpp:72-75), and of the
+    8^3-cell tiles those cells fall in."""
     x = x.astype(np.float32)
     h = rk.astype(np.float32)[:, None]
     L = np.float32(boxsize)
-    tot = 0
+    cells = tiles = 0
     for nc in ncs:
         f = np.float32(nc)
         lo = np.maximum(0, np.trunc(((x - h) / L) * f).astype(np.int64))
         hi = np.minimum(nc, 1 + np.trunc(((x + h) / L) * f).astype(np.int64))
-        tot += int(np.prod(np.maximum(hi - lo, 0), axis=1).sum())
-    return tot
+        ext = np.maximum(hi - lo, 0)
+        cells += int(np.prod(ext, axis=1).sum())
+        t = np.where(ext > 0, (hi - 1) // tile - lo // tile + 1, 0)
+        tiles += int(np.prod(t, axis=1).sum())
+    return cells, tiles
 
 
 def cpu_reference_run(nthreads: int, use_ref: bool):
@@ -276,7 +280,8 @@ def run_ours(args):
     # roofline of the dominant kernel (measured live above)
     fp32 = ctx.measure_fp32_peak()
     pk, pk_kind = peaks()
-    cells = deposit_cells(cube.x, rk_host, cube.boxsize, ncs)
+    cells, tile_pairs = deposit_cells(cube.x, rk_host, cube.boxsize, ncs)
+    dep_stats = ctx.deposit_stats()
     alg = {  # algorithmic FP32 flops per step, per phase
         "knn_t33": 8.0 * 33 * 6 / np.pi * n,  # 8 flops per distance, ~63 candidates per query
         "dens": 14.0 * 32 * n,                 # 14 flops per tent weight, 32 receivers per query
@@ -299,6 +304,8 @@ def run_ours(args):
             "phase_ms_per_step": per_step,
             "alg_flops_per_step": alg,
             "step_alg_hbm_bytes": hbm_alg,
+            "deposit_work": dict(dep_stats, exact_particle_tile_pairs=tile_pairs,
+                                 particle_cell_pairs=cells),
             "step_hbm_gbs_vs_peak": {"achieved": hbm_alg / (ms_step * 1e-3) / 1e9,
                                      "peak": pk["hbm_gbs"], "peak_kind": pk_kind}}
 
