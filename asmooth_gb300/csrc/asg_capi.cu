@@ -47,7 +47,7 @@ struct asg_ctx {
     // loaded particle set
     int n = 0;
     float left = 0.f, right = 0.f;
-    bool loaded = false, knn_done = false, ebox_valid = false;
+    bool loaded = false, knn_done = false, ebox_valid = false, idx33_all = false;
     int* perm = nullptr;       // sorted position -> input index
     uint64_t* keys = nullptr;  // sorted keys
 
@@ -57,7 +57,9 @@ struct asg_ctx {
     Buf uf, minin, mark, scan_tmp, lab_cnt, lab_scan;
     Buf halos, hcount, hmass;
     Buf totals, lohi;
-    Buf dep_lists, dep_counter, dep_ranges, dep_partial;
+    Buf dep_rec, dep_pcount, dep_tiles, dep_counter, dep_pairs, dep_sort, dep_partial;
+    uint32_t dep_npairs = 0;
+    int dep_tiles_n = 0;
     uint32_t* h_u32 = nullptr;  // pinned
     float mesh_boxsize = 0.0f;
     std::vector<MeshBuf> meshes;
@@ -322,8 +324,9 @@ void asg_destroy(asg_ctx* ctx)
                    &ctx->meta, &ctx->parent, &ctx->leaf_parent, &ctx->flags, &ctx->blo,
                    &ctx->bhi, &ctx->elo, &ctx->ehi, &ctx->uf, &ctx->minin, &ctx->mark,
                    &ctx->scan_tmp, &ctx->lab_cnt, &ctx->lab_scan, &ctx->halos, &ctx->hcount,
-                   &ctx->hmass, &ctx->totals, &ctx->lohi, &ctx->dep_lists, &ctx->dep_counter,
-                   &ctx->dep_ranges, &ctx->dep_partial};
+                   &ctx->hmass, &ctx->totals, &ctx->lohi, &ctx->dep_rec, &ctx->dep_pcount,
+                   &ctx->dep_tiles, &ctx->dep_counter, &ctx->dep_pairs, &ctx->dep_sort,
+                   &ctx->dep_partial};
     for (Buf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& m : ctx->meshes) {
@@ -392,12 +395,14 @@ static int run_knn(asg_ctx* ctx)
 {
     const TreeView t = tree_view(ctx);
     phase_begin(ctx, ASG_PH_KNN);
-    launch_knn_t33(P<float4>(ctx->pos), t, P<float>(ctx->t33), ctx->d_err, ctx->s);
+    launch_knn_t33(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<float>(ctx->rk),
+                   P<int>(ctx->idx33), ctx->d_err, ctx->s);
     phase_end(ctx);
-    phase_begin(ctx, ASG_PH_TIES);
-    launch_knn_ties(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33),
-                    P<float>(ctx->rk), ctx->d_err, ctx->s);
+    phase_begin(ctx, ASG_PH_TIES);  // only bundles with an exact tie at the 33rd distance
+    launch_knn_ties(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33), 0,
+                    ctx->d_err, ctx->s);
     phase_end(ctx);
+    ctx->idx33_all = false;
     ctx->ebox_valid = false;
     ensure_ebox(ctx);
     phase_begin(ctx, ASG_PH_DENS);
@@ -574,30 +579,43 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
         tiles += tpd * tpd * tpd;
     }
     if (int r = grow(ctx, ctx->totals, 16 * (size_t)n_nc)) return r;
-    // per-tile candidate lists: count, then size the lists and the work items
+    // particle records and pair counts, then size the pair arrays
+    const int n = ctx->n;
     const size_t T1 = (size_t)tiles + 1;
-    if (int r = grow(ctx, ctx->dep_lists, deposit_list_temp_bytes(tiles))) return r;
+    if (int r = grow(ctx, ctx->dep_rec, deposit_prep_bytes(n))) return r;
+    if (int r = grow(ctx, ctx->dep_pcount, 4 * ((size_t)n + 1) + scan_temp_bytes((size_t)n + 1)))
+        return r;
+    if (int r = grow(ctx, ctx->dep_tiles, deposit_tile_bytes(tiles))) return r;
     if (int r = grow(ctx, ctx->dep_counter, 16)) return r;
     DepositScratch w;
-    w.nranges = P<uint32_t>(ctx->dep_lists);
-    w.nparts = w.nranges + T1;
-    w.range_off = w.nparts + T1;
-    w.item_off = w.range_off + T1;
-    w.scan_tmp = (void*)(w.item_off + T1);
+    w.rec = P<float4>(ctx->dep_rec);
+    w.pcount = P<uint32_t>(ctx->dep_pcount);
+    w.scan_tmp_n = (void*)(w.pcount + n + 1);
+    w.tstart = P<uint32_t>(ctx->dep_tiles);
+    w.tcount = w.tstart + T1;
+    w.item_off = w.tcount + T1;
+    w.scan_tmp_t = (void*)(w.item_off + T1);
     w.next_item = P<int>(ctx->dep_counter);
     phase_begin(ctx, ASG_PH_DEPOSIT);
-    launch_deposit_count(P<float4>(ctx->pos), P<float>(ctx->rk), tree_view(ctx), p, tiles, w,
-                         ctx->d_err, ctx->s);
-    CK(cudaMemcpyAsync(ctx->h_u32, w.range_off + tiles, 4, cudaMemcpyDeviceToHost, ctx->s));
-    CK(cudaMemcpyAsync(ctx->h_u32 + 1, w.item_off + tiles, 4, cudaMemcpyDeviceToHost, ctx->s));
+    launch_deposit_prep(P<float4>(ctx->pos), P<float4>(ctx->vel), P<int>(ctx->igrp),
+                        P<float>(ctx->rk), n, p, w, ctx->d_err, ctx->s);
+    CK(cudaMemcpyAsync(ctx->h_u32, w.pcount + n, 4, cudaMemcpyDeviceToHost, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
-    const uint32_t nranges = ctx->h_u32[0], nitems = ctx->h_u32[1];
-    if (int r = grow(ctx, ctx->dep_ranges, 16 * (size_t)nranges + 16)) return r;
-    if (int r = grow(ctx, ctx->dep_partial, deposit_partial_bytes(nitems) + 16)) return r;
-    w.ranges = P<int4>(ctx->dep_ranges);
+    const uint32_t npairs = ctx->h_u32[0];
+    const size_t NP = (size_t)npairs + 1;
+    if (int r = grow(ctx, ctx->dep_pairs, 16 * NP)) return r;
+    if (int r = grow(ctx, ctx->dep_sort, radix_sort_temp_bytes((int)NP))) return r;
+    const uint32_t max_items = deposit_max_items(tiles, npairs);
+    if (int r = grow(ctx, ctx->dep_partial, deposit_partial_bytes(max_items) + 16)) return r;
+    w.keys0 = P<uint32_t>(ctx->dep_pairs);
+    w.keys1 = w.keys0 + NP;
+    w.vals0 = reinterpret_cast<int*>(w.keys1 + NP);
+    w.vals1 = w.vals0 + NP;
+    w.sort_tmp = ctx->dep_sort.p;
     w.partial = P<float>(ctx->dep_partial);
-    launch_deposit_run(P<float4>(ctx->pos), P<float4>(ctx->vel), P<int>(ctx->igrp),
-                       P<float>(ctx->rk), tree_view(ctx), p, tiles, w, ctx->d_err, ctx->s);
+    ctx->dep_npairs = npairs;
+    ctx->dep_tiles_n = tiles;
+    launch_deposit_run(n, p, tiles, npairs, w, ctx->d_err, ctx->s);
     for (int k = 0; k < n_nc; ++k) {
         const int tpd = (ncs[k] + 7) / 8;
         launch_reduce_partials(P<double>(ctx->meshes[(size_t)k].partial), tpd * tpd * tpd,
@@ -693,6 +711,11 @@ int asg_get_knn(asg_ctx* ctx, float* t33, int* idx33)
     const size_t n = (size_t)ctx->n;
     if (int r = grow(ctx, ctx->uf, 4 * n)) return r;
     if (int r = grow(ctx, ctx->minin, 4 * n)) return r;
+    if (!ctx->idx33_all) {  // the hot path resolves idx33 only where the 33rd value is tied
+        launch_knn_ties(P<float4>(ctx->pos), tree_view(ctx), P<float>(ctx->t33),
+                        P<int>(ctx->idx33), 1, ctx->d_err, ctx->s);
+        ctx->idx33_all = true;
+    }
     launch_scatter_fields(ctx->perm, P<float>(ctx->t33), nullptr, P<int>(ctx->idx33), ctx->n,
                           P<float>(ctx->uf), nullptr, P<int>(ctx->minin), ctx->s);
     if (t33) CK(cudaMemcpyAsync(t33, ctx->uf.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
@@ -842,16 +865,17 @@ __global__ static void k_fma_probe(float* out, int iters, float a, float b)
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-int asg_deposit_stats(asg_ctx* ctx, long long* candidates, long long* buckets, long long* items)
+int asg_deposit_stats(asg_ctx* ctx, long long* pairs, long long* tiles, long long* items)
 {
     if (!ctx) return ASG_ERR_ARG;
     if (!ctx->dep_counter.p) return fail(ctx, ASG_ERR_STATE, "no deposit run yet");
     CK(cudaSetDevice(ctx->device));
-    unsigned long long c = 0;
-    CK(cudaMemcpy(&c, P<char>(ctx->dep_counter) + 8, 8, cudaMemcpyDeviceToHost));
-    if (candidates) *candidates = (long long)c;
-    if (buckets) *buckets = ctx->h_u32[0];
-    if (items) *items = ctx->h_u32[1];
+    uint32_t it = 0;
+    const uint32_t* item_off = P<uint32_t>(ctx->dep_tiles) + 2 * ((size_t)ctx->dep_tiles_n + 1);
+    CK(cudaMemcpy(&it, item_off + ctx->dep_tiles_n, 4, cudaMemcpyDeviceToHost));
+    if (pairs) *pairs = ctx->dep_npairs;
+    if (tiles) *tiles = ctx->dep_tiles_n;
+    if (items) *items = it;
     return ASG_OK;
 }
 

@@ -230,7 +230,8 @@ constexpr int RS_THREADS = 256;
 constexpr int RS_ROUNDS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_count(const uint64_t* __restrict__ keys, int n,
+template <class K>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_count(const K* __restrict__ keys, int n,
                                                          int shift, uint32_t* __restrict__ counts,
                                                          int ntiles)
 {
@@ -251,9 +252,10 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_count(const uint64_t* __restr
     counts[(size_t)threadIdx.x * ntiles + blockIdx.x] = hist[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin,
+template <class K>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const K* __restrict__ kin,
                                                            const int* __restrict__ vin,
-                                                           uint64_t* __restrict__ kout,
+                                                           K* __restrict__ kout,
                                                            int* __restrict__ vout, int n,
                                                            int shift,
                                                            const uint32_t* __restrict__ offs,
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __res
     for (int r = 0; r < RS_ROUNDS; ++r) {
         const int i = base + r * RS_THREADS + threadIdx.x;
         const bool valid = i < n;
-        const uint64_t k = valid ? kin[i] : 0ull;
+        const K k = valid ? kin[i] : (K)0;
         const int v = valid ? vin[i] : 0;
         const unsigned d = valid ? (unsigned)((k >> shift) & 255u) : 256u;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
@@ -305,25 +307,38 @@ size_t radix_sort_temp_bytes(int n)
     return nc * sizeof(uint32_t) + scan_temp_bytes(nc) + 256;
 }
 
-int radix_sort(uint64_t* keys0, int* vals0, uint64_t* keys1, int* vals1, int n, int bits,
-               void* temp, cudaStream_t s)
+template <class K>
+static int radix_sort_t(K* keys0, int* vals0, K* keys1, int* vals1, int n, int bits, void* temp,
+                        cudaStream_t s)
 {
     if (n <= 1) return 0;
     const int ntiles = (n + RS_TILE - 1) / RS_TILE;
     uint32_t* counts = (uint32_t*)temp;
     void* stemp = (void*)(counts + (size_t)256 * ntiles);
-    uint64_t* kb[2] = {keys0, keys1};
+    K* kb[2] = {keys0, keys1};
     int* vb[2] = {vals0, vals1};
     int cur = 0;
     for (int shift = 0; shift < bits; shift += 8) {
-        k_rs_count<<<ntiles, RS_THREADS, 0, s>>>(kb[cur], n, shift, counts, ntiles);
+        k_rs_count<K><<<ntiles, RS_THREADS, 0, s>>>(kb[cur], n, shift, counts, ntiles);
         exclusive_scan_u32(counts, (size_t)256 * ntiles, stemp, s);
-        k_rs_scatter<<<ntiles, RS_THREADS, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n,
-                                                   shift, counts, ntiles);
+        k_rs_scatter<K><<<ntiles, RS_THREADS, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1],
+                                                      n, shift, counts, ntiles);
         count_launches(2);
         cur ^= 1;
     }
     return cur;
+}
+
+int radix_sort(uint64_t* keys0, int* vals0, uint64_t* keys1, int* vals1, int n, int bits,
+               void* temp, cudaStream_t s)
+{
+    return radix_sort_t<uint64_t>(keys0, vals0, keys1, vals1, n, bits, temp, s);
+}
+
+int radix_sort32(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, int n, int bits,
+                 void* temp, cudaStream_t s)
+{
+    return radix_sort_t<uint32_t>(keys0, vals0, keys1, vals1, n, bits, temp, s);
 }
 
 __global__ void k_gather(const int* __restrict__ perm, const float4* __restrict__ pos_in,

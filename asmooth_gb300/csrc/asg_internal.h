@@ -49,6 +49,8 @@ void launch_morton(const float4* pos_in, int n, float left, float right, int* d_
 // stable LSD radix sort of (keys, vals) on the low `bits` bits; ping-pong buffers;
 // returns which buffer (0/1) holds the result
 size_t radix_sort_temp_bytes(int n);
+int radix_sort32(uint32_t* keys0, int* vals0, uint32_t* keys1, int* vals1, int n, int bits,
+                 void* temp, cudaStream_t s);
 int radix_sort(uint64_t* keys0, int* vals0, uint64_t* keys1, int* vals1, int n, int bits,
                void* temp, cudaStream_t s);
 void launch_gather_sorted(const int* perm, const float4* pos_in, const float4* vel_in,
@@ -68,9 +70,12 @@ size_t scan_temp_bytes(size_t n);
 void exclusive_scan_u32(uint32_t* data, size_t n, void* temp, cudaStream_t s);
 
 // ---- neighbour search (asg_knn.cu) -------------------------------------------
-void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, int* err, cudaStream_t s);
+// t33, rk = sqrtf(t33), idx33 = -1 (no tie at the 33rd) or -2 (ties to resolve)
+void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, float* rk, int* idx33,
+                    int* err, cudaStream_t s);
+// idx33 = input index of the 33rd key, for flagged queries (all = 0) or every query
 void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int* idx33,
-                     float* rk, int* err, cudaStream_t s);
+                     int all, int* err, cudaStream_t s);
 // vel[j].w (dens) += the tent weights j receives as one of the 32 nearest
 void launch_dens_gather(const float4* pos, const TreeView& t, const float* t33,
                         const int* idx33, const float* rk, float4* vel, cudaStream_t s);
@@ -95,26 +100,33 @@ struct DepositParams {
     float offset[3];  // periodic: rank cube offset
     int density_only;
 };
-// scratch of one deposit: per-tile candidate lists and work items
+// scratch of one deposit: particle records, (tile, image) pairs, work items
 struct DepositScratch {
-    uint32_t* nranges;    // [T] bucket ranges listed per tile
-    uint32_t* nparts;     // [T] candidate particles per tile
-    uint32_t* range_off;  // [T+1] exclusive scan of nranges
+    float4* rec;          // [4n] x', hinv | (x-h)/L, dens | (x+h)/L, vx | vy, vz, flags
+    uint32_t* pcount;     // [n+1] pairs per particle, then their exclusive scan
+    void* scan_tmp_n;     // scan scratch for n+1 entries
+    uint32_t* keys0;      // [npairs] tile << 5 | image, ping-pong with keys1
+    uint32_t* keys1;
+    int* vals0;           // [npairs] particle (sorted position), ping-pong with vals1
+    int* vals1;
+    void* sort_tmp;       // radix sort scratch for npairs
+    uint32_t* tstart;     // [T] first pair of each tile
+    uint32_t* tcount;     // [T] pairs of each tile
     uint32_t* item_off;   // [T+1] exclusive scan of work items per tile
-    void* scan_tmp;       // scan scratch for T+1 entries
-    int4* ranges;         // [range_off[T]] first, last, flattened start, -
-    float* partial;       // [item_off[T]] partial tiles of multi-segment tiles
+    void* scan_tmp_t;     // scan scratch for T+1 entries
+    float* partial;       // [items] partial tiles of multi-segment tiles
     int* next_item;       // work counter of the persistent kernel
 };
-size_t deposit_list_temp_bytes(int total_tiles);
+size_t deposit_prep_bytes(int n);
+size_t deposit_tile_bytes(int total_tiles);
+uint32_t deposit_max_items(int total_tiles, uint32_t npairs);
 size_t deposit_partial_bytes(uint32_t items);
-// pass 1: count candidates per tile, scan offsets (range_off[T], item_off[T] hold the totals)
-int launch_deposit_count(const float4* pos, const float* rk, const TreeView& t,
-                         const DepositParams& p, int total_tiles, DepositScratch& w, int* err,
+// pass 1: particle records and pair counts; pcount[n] then holds the number of pairs
+void launch_deposit_prep(const float4* pos, const float4* vel, const int* igrp, const float* rk,
+                         int n, const DepositParams& p, DepositScratch& w, int* err,
                          cudaStream_t s);
-// pass 2: fill the lists, deposit every (tile, segment), merge multi-segment tiles
-void launch_deposit_run(const float4* pos, const float4* vel, const int* igrp, const float* rk,
-                        const TreeView& t, const DepositParams& p, int total_tiles,
+// pass 2: emit and sort the pairs, deposit every (tile, segment), merge multi-segment tiles
+void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t npairs,
                         DepositScratch& w, int* err, cudaStream_t s);
 void launch_reduce_partials(const double* partial, int ntiles, double* out2, cudaStream_t s);
 void launch_normalise(float* mesh, int nc, float vol, cudaStream_t s);

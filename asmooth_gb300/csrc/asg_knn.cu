@@ -28,14 +28,19 @@ namespace asg {
 constexpr int KNN_WARPS = 4;
 constexpr unsigned FULL = 0xffffffffu;
 
-__device__ __forceinline__ void insert33(float (&a)[K_NN], float v)
+// min/max insertion of v into the ascending array a[FROM..32]; exact when
+// v >= a[FROM-1] (the lower slots would not change).  Returns the value that
+// drops out (the old a[32] when v < a[32]).
+template <int FROM>
+__device__ __forceinline__ float insert33_from(float (&a)[K_NN], float v)
 {
 #pragma unroll
-    for (int k = 0; k < K_NN; ++k) {
+    for (int k = FROM; k < K_NN; ++k) {
         const float lo = fminf(a[k], v);
         v = fmaxf(a[k], v);
         a[k] = lo;
     }
+    return v;
 }
 
 // squared distance from the query to a child (point for a leaf child)
@@ -49,8 +54,15 @@ __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, con
     return box_dist2_rn(q.x, q.y, q.z, t.blo[c], t.bhi[c]);
 }
 
+// t33 = the 33rd smallest d2 (with multiplicity), rk = sqrtf(t33), and a tie
+// flag: idx33 = -1 when exactly one particle sits at d2 == t33 (then the
+// 32-set is {d2 < t33} and needs no index), -2 when ties must be resolved.
+// The flag tracks whether any particle outside the kept 33 has d2 equal to
+// the current 33rd value: rejected candidates with d2 == a[32], and evicted
+// values equal to the new a[32]; it is cleared whenever a[32] decreases.
 __global__ void __launch_bounds__(KNN_WARPS * 32)
-k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33, int* err)
+k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
+          float* __restrict__ rk, int* __restrict__ idx33, int* err)
 {
     __shared__ int stk[KNN_WARPS][STACK_MAX];
     __shared__ float4 cand[KNN_WARPS][32];
@@ -63,6 +75,7 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33, i
     float a[K_NN];
 #pragma unroll
     for (int k = 0; k < K_NN; ++k) a[k] = INFINITY;
+    bool tie_out = false;  // a particle outside a[] has d2 == a[32]
 
     int* st = stk[warp];
     if (lane == 0) st[0] = tree_root(n);
@@ -80,8 +93,9 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33, i
             if (m.w - m.z + 1 > LEAF_MAX) {
                 const float d0 = child_dist2(pos, t, m.x, xq);
                 const float d1 = child_dist2(pos, t, m.y, xq);
-                const bool v0 = __any_sync(FULL, d0 < a[K_NN - 1]);
-                const bool v1 = __any_sync(FULL, d1 < a[K_NN - 1]);
+                // a node whose distance equals a[32] can hold a tie: visit it
+                const bool v0 = __any_sync(FULL, d0 <= a[K_NN - 1]);
+                const bool v1 = __any_sync(FULL, d1 <= a[K_NN - 1]);
                 const bool c0_near = __popc(__ballot_sync(FULL, d0 <= d1)) >= 16;
                 const int nn = c0_near ? m.x : m.y, ff = c0_near ? m.y : m.x;
                 const bool vn = c0_near ? v0 : v1, vf = c0_near ? v1 : v0;
@@ -98,7 +112,7 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33, i
             last = m.w;
             // thresholds may have shrunk since the push: re-test the bucket
             const float db = box_dist2_rn(xq.x, xq.y, xq.z, t.blo[node], t.bhi[node]);
-            if (!__any_sync(FULL, db < a[K_NN - 1])) continue;
+            if (!__any_sync(FULL, db <= a[K_NN - 1])) continue;
         }
         const int cnt = last - first + 1;
         if (lane < cnt) cand[warp][lane] = pos[first + lane];
@@ -106,8 +120,25 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33, i
         for (int j = 0; j < cnt; ++j) {
             const float4 c = cand[warp][j];
             const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
-            const bool take = d2 < a[K_NN - 1];
-            if (__any_sync(FULL, take)) insert33(a, take ? d2 : INFINITY);
+            const float top = a[K_NN - 1];
+            const bool take = d2 < top;
+            tie_out |= (d2 == top);
+            const unsigned tk = __ballot_sync(FULL, take);
+            if (tk) {
+                const float v = take ? d2 : INFINITY;
+                // shortest exact network: slots below the insertion point do not move
+                float out;
+                if (!__any_sync(FULL, take && d2 < a[K_NN - 5]))
+                    out = insert33_from<K_NN - 5>(a, v);
+                else if (!__any_sync(FULL, take && d2 < a[K_NN - 13]))
+                    out = insert33_from<K_NN - 13>(a, v);
+                else
+                    out = insert33_from<0>(a, v);
+                if (take) {
+                    const float nt = a[K_NN - 1];
+                    tie_out = (nt == top) ? (tie_out || out == nt) : (out == nt);
+                }
+            }
         }
         __syncwarp();
     }
@@ -118,6 +149,8 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33, i
     if (base + lane < n) {
         const float v = a[K_NN - 1];
         t33[base + lane] = v;
+        rk[base + lane] = __fsqrt_rn(v);
+        idx33[base + lane] = (tie_out || a[K_NN - 2] == v) ? -2 : -1;
         if (!(v < INFINITY)) atomicOr(err, ERR_FEW);
         else if (!(v > 0.0f)) atomicOr(err, ERR_ZERO_RK);
     }
@@ -125,7 +158,7 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33, i
 
 __global__ void __launch_bounds__(KNN_WARPS * 32)
 k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
-           int* __restrict__ idx33, float* __restrict__ rk, int* err)
+           int* __restrict__ idx33, int all, int* err)
 {
     __shared__ int stk[KNN_WARPS][STACK_MAX];
     __shared__ float4 cand[KNN_WARPS][32];
@@ -134,6 +167,9 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
     const int base = (blockIdx.x * KNN_WARPS + warp) * 32;
     if (base >= n) return;
     const int q = min(base + lane, n - 1);
+    // unless every index is wanted, only queries flagged by k_knn_t33 (-2) need it
+    const bool want = (base + lane < n) && (all || idx33[q] == -2);
+    if (!__any_sync(FULL, want)) return;
     const float4 xq = pos[q];
     const float T = t33[q];
     int nless = 0, neq = 0;
@@ -194,7 +230,7 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
         if (lane == 0) atomicOr(err, ERR_STACK);
         return;
     }
-    if (base + lane < n) {
+    if (want) {
         const int need = K_NN - nless;  // position of the 33rd key among the ties
         int r = -1;
         if (need < 1 || need > neq) atomicOr(err, ERR_FEW);
@@ -205,7 +241,6 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
                 if (k == need - 1) r = tie[k];
         }
         idx33[base + lane] = r;
-        rk[base + lane] = __fsqrt_rn(T);
     }
 }
 
@@ -297,18 +332,19 @@ k_dens_gather(const float4* __restrict__ pos, TreeView t, const float* __restric
 
 static int knn_blocks(int n) { return (n + KNN_WARPS * 32 - 1) / (KNN_WARPS * 32); }
 
-void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, int* err, cudaStream_t s)
+void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, float* rk, int* idx33,
+                    int* err, cudaStream_t s)
 {
     if (t.n <= 0) return;
-    k_knn_t33<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, err);
+    k_knn_t33<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, rk, idx33, err);
     count_launches(1);
 }
 
 void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int* idx33,
-                     float* rk, int* err, cudaStream_t s)
+                     int all, int* err, cudaStream_t s)
 {
     if (t.n <= 0) return;
-    k_knn_ties<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, rk, err);
+    k_knn_ties<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, all, err);
     count_launches(1);
 }
 

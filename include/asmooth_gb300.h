@@ -168,9 +168,9 @@ const char* asg_phase_name(int phase);
 /* Measured FP32 FMA throughput of this GPU (TFLOP/s, 2 flops per FMA) from a
  * register-resident FMA-chain kernel over all SMs: the FP32 roofline ceiling. */
 int asg_measure_fp32_peak(asg_ctx* ctx, double* tflops);
-/* Work statistics of the last deposit: candidate particle-tile pairs listed,
- * tree buckets listed, work items run. */
-int asg_deposit_stats(asg_ctx* ctx, long long* candidates, long long* buckets, long long* items);
+/* Work statistics of the last deposit: (particle, 8^3-cell tile) pairs
+ * deposited, mesh tiles, work items run. */
+int asg_deposit_stats(asg_ctx* ctx, long long* pairs, long long* tiles, long long* items);
 
 #ifdef __cplusplus
 }
