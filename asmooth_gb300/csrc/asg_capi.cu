@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -48,6 +49,7 @@ struct asg_ctx {
     int n = 0;
     float left = 0.f, right = 0.f;
     bool loaded = false, knn_done = false, ebox_valid = false, idx33_all = false;
+    int leaf = 16;  // tree bucket size scanned whole by the traversals
     int* perm = nullptr;       // sorted position -> input index
     uint64_t* keys = nullptr;  // sorted keys
 
@@ -182,6 +184,7 @@ TreeView tree_view(asg_ctx* ctx)
 {
     TreeView t;
     t.n = ctx->n;
+    t.leaf = ctx->leaf;
     t.meta = P<int4>(ctx->meta);
     t.blo = P<float4>(ctx->blo);
     t.bhi = P<float4>(ctx->bhi);
@@ -297,6 +300,10 @@ int asg_create(asg_ctx** out, int device)
     *out = nullptr;
     asg_ctx* ctx = new asg_ctx();
     ctx->device = device;
+    if (const char* e = std::getenv("ASG_LEAF_SIZE")) {  // tuning knob (1..32)
+        const int v = std::atoi(e);
+        if (v >= 1 && v <= LEAF_MAX) ctx->leaf = v;
+    }
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));

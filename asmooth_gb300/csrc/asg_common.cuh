@@ -13,7 +13,7 @@
 namespace asg {
 
 constexpr int K_NN = 33;        // KNeighbors::k (k_neighbors.h:47): 32 neighbours + self
-constexpr int LEAF_MAX = 32;    // a tree node with <= 32 particles is scanned as a bucket
+constexpr int LEAF_MAX = 32;    // largest bucket: a tree node with <= leaf particles (leaf <= 32) is scanned whole
 constexpr int STACK_MAX = 128;  // traversal stack entries per warp
 constexpr int TIE_MAX = 16;     // exact d2 ties tracked at the 33rd neighbour
 

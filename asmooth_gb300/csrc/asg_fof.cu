@@ -75,7 +75,7 @@ k_fof_link(const float4* __restrict__ pos, TreeView t, float ll2, int* P, int* e
             first = last = ~node;
         } else {
             const int4 m = t.meta[node];
-            if (m.w - m.z + 1 > LEAF_MAX) {
+            if (m.w - m.z + 1 > t.leaf) {
                 auto need = [&](int c) {
                     // only partners with a larger sorted position are linked from q
                     if (c < 0) return active && ~c > q;
@@ -249,7 +249,7 @@ k_mark_halos(const float4* __restrict__ pos, TreeView t, const float* __restrict
         } else {
             const int4 m = t.meta[node];
             if (box_dist2_rn(cx, cy, cz, t.blo[node], t.bhi[node]) >= r2) continue;
-            if (m.w - m.z + 1 > LEAF_MAX) {
+            if (m.w - m.z + 1 > t.leaf) {
                 if (sp + 2 > STACK_MAX) { overflow = true; break; }
                 if (lane == 0) { st[sp] = m.y; st[sp + 1] = m.x; }
                 sp += 2;

@@ -23,6 +23,7 @@ void count_launches(int k);
 
 struct TreeView {
     int n;                 // particles (leaves)
+    int leaf;              // bucket size: nodes with <= leaf particles are scanned whole (1..32)
     const int4* meta;      // internal nodes 0..n-2 (root 0); empty when n == 1
     const float4* blo;
     const float4* bhi;

@@ -60,7 +60,7 @@ __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, con
 // The flag tracks whether any particle outside the kept 33 has d2 equal to
 // the current 33rd value: rejected candidates with d2 == a[32], and evicted
 // values equal to the new a[32]; it is cleared whenever a[32] decreases.
-__global__ void __launch_bounds__(KNN_WARPS * 32)
+__global__ void __launch_bounds__(KNN_WARPS * 32, 8)
 k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
           float* __restrict__ rk, int* __restrict__ idx33, int* err)
 {
@@ -90,7 +90,7 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             first = last = ~node;
         } else {
             const int4 m = t.meta[node];
-            if (m.w - m.z + 1 > LEAF_MAX) {
+            if (m.w - m.z + 1 > t.leaf) {
                 const float d0 = child_dist2(pos, t, m.x, xq);
                 const float d1 = child_dist2(pos, t, m.y, xq);
                 // a node whose distance equals a[32] can hold a tie: visit it
@@ -123,17 +123,8 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             const float top = a[K_NN - 1];
             const bool take = d2 < top;
             tie_out |= (d2 == top);
-            const unsigned tk = __ballot_sync(FULL, take);
-            if (tk) {
-                const float v = take ? d2 : INFINITY;
-                // shortest exact network: slots below the insertion point do not move
-                float out;
-                if (!__any_sync(FULL, take && d2 < a[K_NN - 5]))
-                    out = insert33_from<K_NN - 5>(a, v);
-                else if (!__any_sync(FULL, take && d2 < a[K_NN - 13]))
-                    out = insert33_from<K_NN - 13>(a, v);
-                else
-                    out = insert33_from<0>(a, v);
+            if (__any_sync(FULL, take)) {
+                const float out = insert33_from<0>(a, take ? d2 : INFINITY);
                 if (take) {
                     const float nt = a[K_NN - 1];
                     tie_out = (nt == top) ? (tie_out || out == nt) : (out == nt);
@@ -190,7 +181,7 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
             first = last = ~node;
         } else {
             const int4 m = t.meta[node];
-            if (m.w - m.z + 1 > LEAF_MAX) {
+            if (m.w - m.z + 1 > t.leaf) {
                 const bool v0 = __any_sync(FULL, child_dist2(pos, t, m.x, xq) <= T);
                 const bool v1 = __any_sync(FULL, child_dist2(pos, t, m.y, xq) <= T);
                 if (sp + 2 > STACK_MAX) { overflow = true; break; }
@@ -287,7 +278,7 @@ k_dens_gather(const float4* __restrict__ pos, TreeView t, const float* __restric
             first = last = ~node;
         } else {
             const int4 m = t.meta[node];
-            if (m.w - m.z + 1 > LEAF_MAX) {
+            if (m.w - m.z + 1 > t.leaf) {
                 const bool v0 = __any_sync(FULL, child_in(m.x));
                 const bool v1 = __any_sync(FULL, child_in(m.y));
                 if (sp + 2 > STACK_MAX) break;  // k_knn_t33 already flagged the same tree
