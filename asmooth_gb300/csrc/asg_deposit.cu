@@ -228,10 +228,11 @@ struct DepShared {
     float4 accB[TS][TS * TS];  // vx, vy, vz, halo_hi
     float accC[TS][TS * TS];   // halo_lo
     int item, tile;
-    int rect[CH][6];           // tile-relative [x0,x1) [y0,y1) [z0,z1); x0 >= x1 when unused
+    // rows padded to odd word strides so that lane-indexed rows hit distinct banks
+    int rect[CH][7];           // tile-relative [x0,x1) [y0,y1) [z0,z1); x0 >= x1 when unused
     float4 val[CH];            // dens, vx, vy, vz
     int halo[CH];
-    float w[CH][3][TS];        // 1-D cell weights of the pair's image over the tile's cells
+    float w[CH][3 * TS + 3];   // 1-D cell weights of the pair's image: [a * (TS+1) + cell]
     double red[2][DEP_THREADS / 32];
 };
 
@@ -363,7 +364,7 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                         for (int t = r0; t < r1; ++t) {
                             const int ii = t + sh;  // unwrapped cell index
                             const float s1 = __fmul_rn(__fsub_rn(__fmul_rn((float)ii, J.dx), xs[a]), hinv);
-                            S.w[tid][a][t] = ker_integ_rn(s1, __fadd_rn(s1, ds));
+                            S.w[tid][a * (TS + 1) + t] = ker_integ_rn(s1, __fadd_rn(s1, ds));
                         }
                     }
                     S.val[tid] = make_float4(B.w, Cc.w, D.x, D.y);
@@ -387,12 +388,12 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                         const int y0 = S.rect[p][2], y1 = S.rect[p][3];
                         const int nx = x1 - x0;
                         const int ncell = nx * (y1 - y0);
-                        const float kz = S.w[p][2][warp];
+                        const float kz = S.w[p][2 * (TS + 1) + warp];
                         const float4 val = S.val[p];
                         const int hal = S.halo[p];
                         for (int c = lane; c < ncell; c += 32) {
                             const int ix = x0 + c % nx, iy = y0 + c / nx;
-                            const float w3 = __fmul_rn(__fmul_rn(S.w[p][0][ix], S.w[p][1][iy]), kz);
+                            const float w3 = __fmul_rn(__fmul_rn(S.w[p][ix], S.w[p][(TS + 1) + iy]), kz);
                             const int cell = iy * TS + ix;
                             if (!hal) {
                                 float4 Aa = S.accA[warp][cell];

@@ -124,11 +124,10 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             const bool take = d2 < top;
             tie_out |= (d2 == top);
             if (__any_sync(FULL, take)) {
-                const float out = insert33_from<0>(a, take ? d2 : INFINITY);
-                if (take) {
-                    const float nt = a[K_NN - 1];
-                    tie_out = (nt == top) ? (tie_out || out == nt) : (out == nt);
-                }
+                insert33_from<0>(a, take ? d2 : INFINITY);
+                // the value that dropped out is the old a[32]: a tie remains exactly
+                // when the new a[32] still equals it
+                if (take) tie_out = (a[K_NN - 1] == top);
             }
         }
         __syncwarp();
