@@ -49,7 +49,7 @@ struct asg_ctx {
     int n = 0;
     float left = 0.f, right = 0.f;
     bool loaded = false, knn_done = false, ebox_valid = false, idx33_all = false;
-    int leaf = 16;  // tree bucket size scanned whole by the traversals
+    int leaf = 32;  // tree bucket size scanned whole by the traversals (fastest on GB300)
     int* perm = nullptr;       // sorted position -> input index
     uint64_t* keys = nullptr;  // sorted keys
 
