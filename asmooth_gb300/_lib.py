@@ -49,6 +49,7 @@ SIGNATURES = {
     "asg_phase_name": (C.c_char_p, [_i]),
     "asg_measure_fp32_peak": (_i, [_vp, _dp]),
     "asg_deposit_stats": (_i, [_vp, _vp, _vp, _vp]),
+    "asg_neighbor_search_noalloc": (_i, [_vp, _i, _f, _f, _vp, _vp, _vp]),
 }
 NPHASES = 8
 

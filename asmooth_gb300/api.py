@@ -35,6 +35,7 @@ ASG_OK = 0
 ASG_ERR_ARG, ASG_ERR_CUDA, ASG_ERR_NOMEM, ASG_ERR_FEW, ASG_ERR_ZERO_RK = -1, -2, -3, -4, -5
 ASG_ERR_NONFINITE, ASG_ERR_STACK, ASG_ERR_TIES, ASG_ERR_RANGE, ASG_ERR_STATE = -6, -7, -8, -9, -10
 ASG_ERR_UNIONFIND = -11
+ASG_ERR_NOALLOC_LIMIT = -12
 
 
 class AsmoothError(RuntimeError):

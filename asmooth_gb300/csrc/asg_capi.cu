@@ -288,6 +288,7 @@ const char* asg_strerror(int status)
     case ASG_ERR_RANGE: return "periodic kernel support wider than the mesh";
     case ASG_ERR_STATE: return "call order: a required previous step is missing";
     case ASG_ERR_UNIONFIND: return "union-find retry limit reached";
+    case ASG_ERR_NOALLOC_LIMIT: return "input larger than the allocation-free entry point's scratch";
     default: return "unknown status";
     }
 }

@@ -49,7 +49,8 @@ enum {
     ASG_ERR_TIES = -8,        /* more than 16 particles tied exactly at the 33rd distance */
     ASG_ERR_RANGE = -9,       /* periodic deposit: kernel support wider than the mesh */
     ASG_ERR_STATE = -10,      /* call needs a previous step (e.g. deposit before search) */
-    ASG_ERR_UNIONFIND = -11   /* FOF union-find retry limit reached */
+    ASG_ERR_UNIONFIND = -11,  /* FOF union-find retry limit reached */
+    ASG_ERR_NOALLOC_LIMIT = -12 /* input larger than the allocation-free entry point's fixed scratch */
 };
 
 /* ---- context ------------------------------------------------------------- */
@@ -171,6 +172,25 @@ int asg_measure_fp32_peak(asg_ctx* ctx, double* tflops);
 /* Work statistics of the last deposit: (particle, 8^3-cell tile) pairs
  * deposited, mesh tiles, work items run. */
 int asg_deposit_stats(asg_ctx* ctx, long long* pairs, long long* tiles, long long* items);
+
+/* ---- allocation-free neighbour search -------------------------------------------- */
+/* No counterpart in the reference: an entry point for callers that cannot
+ * allocate device memory, for example a host application whose memory manager
+ * reserves the whole GPU up front and lends libraries only its own buffers.
+ * Same results as asg_neighbor_search (rk = sqrtf of the 33rd neighbour d2,
+ * tent weights added to dens), but inputs and outputs are the caller's device
+ * arrays: d_x (np*3 floats), d_rk (np floats, written), d_dens (np floats,
+ * added to).  The scratch is a fixed array inside the library, present on
+ * every GPU that loads it until the process exits, so the call makes no
+ * cudaMalloc/cudaFree.  Limits: 33 <= np <= ASG_NOALLOC_MAX_PARTICLES (larger
+ * inputs return ASG_ERR_NOALLOC_LIMIT).  All calls on one device share that
+ * scratch: calls that overlap on the GPU race, so serialise them.  The first
+ * call on each device looks up the scratch's device address; make it before
+ * any stream capture.  stream may be NULL (the default stream); the call
+ * returns when the work on stream is complete. */
+#define ASG_NOALLOC_MAX_PARTICLES 32768
+int asg_neighbor_search_noalloc(const float* d_x, int np, float left, float right, float* d_rk,
+                                float* d_dens, void* stream);
 
 #ifdef __cplusplus
 }
