@@ -18,11 +18,12 @@
 //      an exclusive scan (so the emit order is the particle order).
 //  (3) a stable radix sort of the pairs by key = tile << 5 | image groups each
 //      tile's particles in particle order.
-//  (4) k_deposit_items: a persistent kernel takes (tile, segment of SEG
-//      pairs) work items; a CTA accumulates a shared-memory tile in which warp
-//      w owns z-layer w and adds one particle after another, so every cell sums
-//      its contributions in list order.  k_merge_tiles adds the partial tiles
-//      of multi-segment tiles in segment order.
+//  (4) k_deposit_items: a persistent kernel whose warps take (tile, segment
+//      of SEG pairs) work items; a warp accumulates its item in a private
+//      shared-memory tile and adds one pair after another, its lanes over the
+//      pair's 3-D cell box, so every cell sums its contributions in list
+//      order.  k_merge_tiles adds the partial tiles of multi-segment tiles in
+//      segment order.
 // n, c and halo are double-float (two-sum) sums, so the per-tile FP64 totals
 // reproduce the FP64 sum of the float weights.
 #include "asg_common.cuh"
@@ -32,8 +33,7 @@ namespace asg {
 
 constexpr int TS = 8;              // tile edge in cells
 constexpr int TC = TS * TS * TS;   // cells per tile
-constexpr int DEP_THREADS = 256;   // 8 warps: warp w <-> z-layer w
-constexpr int CH = 256;            // pairs per processing chunk (one per thread)
+constexpr int DEP_THREADS = 256;   // threads of the tile-merge CTA
 constexpr int SEG = 4096;          // pairs per work item
 constexpr int PW = 9;              // partial words per cell
 constexpr int IMG_BITS = 5;        // periodic images per pair: up to 3 x 3 x 3
@@ -223,18 +223,41 @@ __global__ void k_tile_items(const uint32_t* __restrict__ tstart, uint32_t* __re
 // ---------------------------------------------------------------------------
 // (4) persistent deposit of (tile, segment) work items
 // ---------------------------------------------------------------------------
-struct DepShared {
-    float4 accA[TS][TS * TS];  // n_hi, n_lo, c_hi, c_lo
-    float4 accB[TS][TS * TS];  // vx, vy, vz, halo_hi
-    float accC[TS][TS * TS];   // halo_lo
-    int item, tile;
-    // rows padded to odd word strides so that lane-indexed rows hit distinct banks
-    int rect[CH][7];           // tile-relative [x0,x1) [y0,y1) [z0,z1); x0 >= x1 when unused
-    float4 val[CH];            // dens, vx, vy, vz
-    int halo[CH];
-    float w[CH][3 * TS + 3];   // 1-D cell weights of the pair's image: [a * (TS+1) + cell]
-    double red[2][DEP_THREADS / 32];
+// One warp owns one work item and accumulates its tile in a private
+// shared-memory copy; it adds the item's pairs one after another, its lanes
+// spread over the pair's whole 3-D cell box.  Per cell the additions happen in
+// pair order, so the sums are deterministic.
+constexpr int DEP_WARPS = 2;                // warps per CTA (independent)
+constexpr int WROW = 3 * TS + 1;            // staged 1-D weights per lane: [axis * TS + cell]
+
+struct WarpTile {
+    float4 a[TC];           // n_hi, n_lo, c_hi, c_lo
+    float4 b[TC];           // vx, vy, vz, halo_hi
+    float hl[TC];           // halo_lo
+    float w[32][WROW];      // 1-D cell weights of the chunk's 32 pairs (odd row stride)
 };
+
+// cell slot in a WarpTile: rows of 8 cells rotated by (6y + 4z) mod 8, which
+// spreads the 128-bit accesses of a small 3-D box over distinct bank groups
+__device__ __forceinline__ int tile_slot(int x, int y, int z)
+{
+    return (z << 6) | (y << 3) | ((x + 6 * y + 4 * z) & (TS - 1));
+}
+
+// 1/d rounded to nearest, d = 0..64: floor(c / d) = trunc((c + 0.5) * (1/d))
+// exactly for 0 <= c < 4096 (checked for every c and d in float32)
+#define ASG_R(d) (1.0f / (float)(d))
+#define ASG_R8(b) ASG_R(b + 1), ASG_R(b + 2), ASG_R(b + 3), ASG_R(b + 4), ASG_R(b + 5), \
+    ASG_R(b + 6), ASG_R(b + 7), ASG_R(b + 8)
+__constant__ float c_rcp[TS * TS + 1] = {0.0f, ASG_R8(0), ASG_R8(8), ASG_R8(16), ASG_R8(24),
+                                         ASG_R8(32), ASG_R8(40), ASG_R8(48), ASG_R8(56)};
+#undef ASG_R8
+#undef ASG_R
+
+__device__ __forceinline__ int small_div(int c, float rcp)
+{
+    return __float2int_rz(__fmul_rn(__fadd_rn(__int2float_rn(c), 0.5f), rcp));
+}
 
 __device__ __forceinline__ int upper_index(const uint32_t* __restrict__ a, int n, uint32_t v)
 {
@@ -247,19 +270,19 @@ __device__ __forceinline__ int upper_index(const uint32_t* __restrict__ a, int n
     return lo;
 }
 
-__device__ __forceinline__ void write_tile(DepShared& S, const DepositParams& P, const TileGeo& g,
-                                           double& sn, double& sh, int tid)
+__device__ __forceinline__ void write_tile(const WarpTile& S, const DepositParams& P, const TileGeo& g,
+                                           double& sn, double& sh, int lane)
 {
     const MeshJob& J = P.job[g.job];
     const int nc = g.nc;
     const size_t nmesh = (size_t)nc * nc * nc;
-    for (int e = tid; e < TC; e += DEP_THREADS) {
-        const int lz = e / (TS * TS), c = e % (TS * TS);
-        const int lx = c % TS, ly = c / TS;
+    for (int e = lane; e < TC; e += 32) {
+        const int lz = e >> 6, ly = (e >> 3) & (TS - 1), lx = e & (TS - 1);
         if (lx >= g.E[0] || ly >= g.E[1] || lz >= g.E[2]) continue;
-        const float4 A = S.accA[lz][c];
-        const float4 B = S.accB[lz][c];
-        const float hl = S.accC[lz][c];
+        const int slot = tile_slot(lx, ly, lz);
+        const float4 A = S.a[slot];
+        const float4 B = S.b[slot];
+        const float hl = S.hl[slot];
         const size_t idx = ((size_t)(g.O[2] + lz) * nc + (g.O[1] + ly)) * nc + (g.O[0] + lx);
         sn += (double)A.x + (double)A.y;
         sh += (double)B.w + (double)hl;
@@ -299,7 +322,7 @@ __device__ __forceinline__ void block_totals(double sn, double sh, double (*red)
     }
 }
 
-__global__ void __launch_bounds__(DEP_THREADS)
+__global__ void __launch_bounds__(32 * DEP_WARPS)
 k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                 const uint32_t* __restrict__ item_off, const uint32_t* __restrict__ tstart,
                 const uint32_t* __restrict__ tcount, const uint32_t* __restrict__ pkeys,
@@ -307,19 +330,19 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                 int* __restrict__ next_item)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    DepShared& S = *reinterpret_cast<DepShared*>(smem_raw);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int lane = threadIdx.x & 31;
+    WarpTile& S = reinterpret_cast<WarpTile*>(smem_raw)[threadIdx.x >> 5];
     const bool periodic = P.periodic != 0;
     const uint32_t total_items = item_off[total_tiles];
 
     for (;;) {
-        if (tid == 0) {
-            const int it = atomicAdd(next_item, 1);
-            S.item = it;
-            S.tile = (uint32_t)it < total_items ? upper_index(item_off, total_tiles + 1, (uint32_t)it) : -1;
+        int item = 0, tile = -1;
+        if (lane == 0) {
+            item = atomicAdd(next_item, 1);
+            if ((uint32_t)item < total_items) tile = upper_index(item_off, total_tiles + 1, (uint32_t)item);
         }
-        __syncthreads();
-        const int item = S.item, tile = S.tile;
+        item = __shfl_sync(FULLM, item, 0);
+        tile = __shfl_sync(FULLM, tile, 0);
         if ((uint32_t)item >= total_items) break;
         const TileGeo g = tile_geo(P, tile);
         const MeshJob& J = P.job[g.job];
@@ -329,17 +352,21 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
         const int j0 = (int)tstart[tile] + seg * SEG;
         const int j1 = (int)tstart[tile] + min((int)tcount[tile], (seg + 1) * SEG);
 
-        for (int e = tid; e < TC; e += DEP_THREADS) {
-            (&S.accA[0][0])[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-            (&S.accB[0][0])[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-            (&S.accC[0][0])[e] = 0.f;
+        for (int e = lane; e < TC; e += 32) {
+            S.a[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+            S.b[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+            S.hl[e] = 0.f;
         }
+        __syncwarp();
 
-        for (int c0 = j0; c0 < j1; c0 += CH) {
-            // ---- setup: one pair per thread: exact ranges of its image, 1-D weights ----
+        for (int c0 = j0; c0 < j1; c0 += 32) {
+            // ---- setup: one pair per lane: exact ranges of its image, 1-D weights ----
+            // rect packs tile-relative [x0,x1) [y0,y1) [z0,z1) in 4-bit fields and
+            // the halo flag in bit 24; 0 means no cells
+            uint32_t rect = 0;
+            float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
             {
-                const int j = c0 + tid;
-                int r[6] = {0, 0, 0, 0, 0, 0};
+                const int j = c0 + lane;
                 if (j < j1) {
                     const int i = pvals[j];
                     const int combo = (int)(pkeys[j] & ((1u << IMG_BITS) - 1u));
@@ -353,91 +380,106 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                     const float hi[3] = {Cc.x, Cc.y, Cc.z};
                     const float hinv = A.w;
                     const float ds = __fmul_rn(J.dx, hinv);  // coarse_mesh.cpp:80
+                    float* wl = S.w[lane];
+                    uint32_t r = 0;
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
                         const AxisRange ar = axis_range(lo[a], hi[a], J, nc, periodic);
                         const int k = ar.k_lo + dk[a];
                         const int sh = k * nc + g.O[a];
                         const int r0 = max(ar.left - sh, 0), r1 = min(ar.right - sh, g.E[a]);
-                        r[2 * a] = r0;
-                        r[2 * a + 1] = r1;
+                        r |= (uint32_t)((r0 & 15) | ((max(r1, r0) & 15) << 4)) << (8 * a);
                         for (int t = r0; t < r1; ++t) {
                             const int ii = t + sh;  // unwrapped cell index
                             const float s1 = __fmul_rn(__fsub_rn(__fmul_rn((float)ii, J.dx), xs[a]), hinv);
-                            S.w[tid][a * (TS + 1) + t] = ker_integ_rn(s1, __fadd_rn(s1, ds));
+                            wl[a * TS + t] = ker_integ_rn(s1, __fadd_rn(s1, ds));
                         }
                     }
-                    S.val[tid] = make_float4(B.w, Cc.w, D.x, D.y);
-                    S.halo[tid] = __float_as_int(D.z) & FLAG_HALO;
+                    rect = r | ((uint32_t)(__float_as_int(D.z) & FLAG_HALO) << 24);
+                    val = make_float4(B.w, Cc.w, D.x, D.y);
                 }
-#pragma unroll
-                for (int a = 0; a < 6; ++a) S.rect[tid][a] = r[a];
             }
-            __syncthreads();
-            // ---- warp w deposits every pair of the chunk that touches z-layer w, in order ----
-            if (warp < g.E[2]) {
-                for (int grp = 0; grp < CH / 32; ++grp) {
-                    const int pl = grp * 32 + lane;
-                    const bool mine = S.rect[pl][0] < S.rect[pl][1] && warp >= S.rect[pl][4] &&
-                                      warp < S.rect[pl][5];
-                    unsigned mask = __ballot_sync(FULLM, mine);
-                    while (mask) {
-                        const int p = grp * 32 + __ffs(mask) - 1;
-                        mask &= mask - 1;
-                        const int x0 = S.rect[p][0], x1 = S.rect[p][1];
-                        const int y0 = S.rect[p][2], y1 = S.rect[p][3];
-                        const int nx = x1 - x0;
-                        const int ncell = nx * (y1 - y0);
-                        const float kz = S.w[p][2 * (TS + 1) + warp];
-                        const float4 val = S.val[p];
-                        const int hal = S.halo[p];
-                        for (int c = lane; c < ncell; c += 32) {
-                            const int ix = x0 + c % nx, iy = y0 + c / nx;
-                            const float w3 = __fmul_rn(__fmul_rn(S.w[p][ix], S.w[p][(TS + 1) + iy]), kz);
-                            const int cell = iy * TS + ix;
-                            if (!hal) {
-                                float4 Aa = S.accA[warp][cell];
-                                float4 Bb = S.accB[warp][cell];
-                                two_sum_acc(Aa.x, Aa.y, w3);
-                                const float pr = __fmul_rn(w3, val.x);
-                                const float pe = fmaf(w3, val.x, -pr);
-                                two_sum_acc(Aa.z, Aa.w, pr);
-                                Aa.w = __fadd_rn(Aa.w, pe);
-                                Bb.x = fmaf(w3, val.y, Bb.x);
-                                Bb.y = fmaf(w3, val.z, Bb.y);
-                                Bb.z = fmaf(w3, val.w, Bb.z);
-                                S.accA[warp][cell] = Aa;
-                                S.accB[warp][cell] = Bb;
-                            } else {
-                                float hh = S.accB[warp][cell].w, hl = S.accC[warp][cell];
-                                two_sum_acc(hh, hl, w3);
-                                S.accB[warp][cell].w = hh;
-                                S.accC[warp][cell] = hl;
-                            }
-                        }
+            __syncwarp();
+            // ---- the warp adds the chunk's pairs in order, lanes over each pair's cells ----
+            const int cnt = min(32, j1 - c0);
+            for (int p = 0; p < cnt; ++p) {
+                const uint32_t rp = __shfl_sync(FULLM, rect, p);
+                const int x0 = rp & 15, nx = ((rp >> 4) & 15) - x0;
+                const int y0 = (rp >> 8) & 15, ny = ((rp >> 12) & 15) - y0;
+                const int z0 = (rp >> 16) & 15, nz = ((rp >> 20) & 15) - z0;
+                if (nx <= 0 || ny <= 0 || nz <= 0) continue;
+                const float dens = __shfl_sync(FULLM, val.x, p);
+                const float vx = __shfl_sync(FULLM, val.y, p);
+                const float vy = __shfl_sync(FULLM, val.z, p);
+                const float vz = __shfl_sync(FULLM, val.w, p);
+                const int nxy = nx * ny, ncell = nxy * nz;
+                const float rx = c_rcp[nx], rxy = c_rcp[nxy];
+                const float* wp = S.w[p];
+                if (!(rp >> 24)) {
+                    for (int c = lane; c < ncell; c += 32) {
+                        const int iz = small_div(c, rxy);
+                        const int rem = c - iz * nxy;
+                        const int iy = small_div(rem, rx);
+                        const int gx = x0 + rem - iy * nx, gy = y0 + iy, gz = z0 + iz;
+                        const float w3 = __fmul_rn(__fmul_rn(wp[gx], wp[TS + gy]), wp[2 * TS + gz]);
+                        const int slot = tile_slot(gx, gy, gz);
+                        float4 Aa = S.a[slot];
+                        float4 Bb = S.b[slot];
+                        two_sum_acc(Aa.x, Aa.y, w3);
+                        const float pr = __fmul_rn(w3, dens);
+                        const float pe = fmaf(w3, dens, -pr);
+                        two_sum_acc(Aa.z, Aa.w, pr);
+                        Aa.w = __fadd_rn(Aa.w, pe);
+                        Bb.x = fmaf(w3, vx, Bb.x);
+                        Bb.y = fmaf(w3, vy, Bb.y);
+                        Bb.z = fmaf(w3, vz, Bb.z);
+                        S.a[slot] = Aa;
+                        S.b[slot] = Bb;
+                    }
+                } else {
+                    for (int c = lane; c < ncell; c += 32) {
+                        const int iz = small_div(c, rxy);
+                        const int rem = c - iz * nxy;
+                        const int iy = small_div(rem, rx);
+                        const int gx = x0 + rem - iy * nx, gy = y0 + iy, gz = z0 + iz;
+                        const float w3 = __fmul_rn(__fmul_rn(wp[gx], wp[TS + gy]), wp[2 * TS + gz]);
+                        const int slot = tile_slot(gx, gy, gz);
+                        float hh = S.b[slot].w, hl = S.hl[slot];
+                        two_sum_acc(hh, hl, w3);
+                        S.b[slot].w = hh;
+                        S.hl[slot] = hl;
                     }
                 }
+                __syncwarp();  // the next pair may add to the same cells from other lanes
             }
-            __syncthreads();
+            __syncwarp();  // the next chunk's setup overwrites S.w
         }
 
         // ---- write: final tile when alone, partial tile otherwise ----
         if (nseg > 1) {
             float* pt = partial + (size_t)item * TC * PW;
-            for (int e = tid; e < TC; e += DEP_THREADS) {
-                const int lz = e / (TS * TS), c = e % (TS * TS);
-                const float4 A = S.accA[lz][c];
-                const float4 B = S.accB[lz][c];
+            for (int e = lane; e < TC; e += 32) {
+                const int slot = tile_slot(e & (TS - 1), (e >> 3) & (TS - 1), e >> 6);
+                const float4 A = S.a[slot];
+                const float4 B = S.b[slot];
                 pt[e] = A.x; pt[TC + e] = A.y; pt[2 * TC + e] = A.z; pt[3 * TC + e] = A.w;
                 pt[4 * TC + e] = B.x; pt[5 * TC + e] = B.y; pt[6 * TC + e] = B.z;
-                pt[7 * TC + e] = B.w; pt[8 * TC + e] = S.accC[lz][c];
+                pt[7 * TC + e] = B.w; pt[8 * TC + e] = S.hl[slot];
             }
         } else {
             double sn = 0.0, sh = 0.0;
-            write_tile(S, P, g, sn, sh, tid);
-            block_totals(sn, sh, S.red, J, g.local, tid);
+            write_tile(S, P, g, sn, sh, lane);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sn += __shfl_down_sync(FULLM, sn, o);
+                sh += __shfl_down_sync(FULLM, sh, o);
+            }
+            if (lane == 0) {
+                J.partial[2 * g.local] = sn;
+                J.partial[2 * g.local + 1] = sh;
+            }
         }
-        __syncthreads();
+        __syncwarp();  // the next item clears the tile
     }
 }
 
@@ -541,19 +583,20 @@ void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t
     k_tile_items<<<(T + 1 + 255) / 256, 256, 0, s>>>(w.tstart, w.tcount, T, w.item_off);
     exclusive_scan_u32(w.item_off, (size_t)T + 1, w.scan_tmp_t, s);
     cudaMemsetAsync(w.next_item, 0, sizeof(int), s);
-    const size_t smem = sizeof(DepShared);
+    const size_t smem = DEP_WARPS * sizeof(WarpTile);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_deposit_items, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_deposit_items, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         attr = true;
     }
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_items, DEP_THREADS, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_items, 32 * DEP_WARPS, smem);
     const int grid = sms * (per_sm > 0 ? per_sm : 1);
-    k_deposit_items<<<grid, DEP_THREADS, smem, s>>>(w.rec, p, T, w.item_off, w.tstart, w.tcount,
-                                                    keys, vals, w.partial, w.next_item);
+    k_deposit_items<<<grid, 32 * DEP_WARPS, smem, s>>>(w.rec, p, T, w.item_off, w.tstart, w.tcount,
+                                                       keys, vals, w.partial, w.next_item);
     k_merge_tiles<<<T, DEP_THREADS, 0, s>>>(p, T, w.item_off, w.partial);
     count_launches(3);
 }
