@@ -290,13 +290,14 @@ def run_ours(args):
     per_step = {k: v / args.steps for k, v in phases.items()}
     dom = max(("knn_t33", "deposit", "dens"), key=lambda k: per_step.get(k, 0.0))
     achieved = alg[dom] / (per_step[dom] * 1e-3) / 1e12
+    # DRAM bytes of one launch of the dominant kernel: the per-particle figure of
+    # an ncu capture of a smaller cube, times this launch's particles
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
     if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get(dom)
-        except Exception:
-            traffic = None
+        rec = json.load(open(tpath)).get(dom)
+        if rec:
+            traffic = rec["bytes_per_particle"] * n
     hbm_alg = n * (12 + 8 + 36) + sum(24 * nc ** 3 for nc in ncs)
     roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": fp32, "unit": "TFLOP/s",
             "frac": achieved / fp32, "traffic": traffic,
