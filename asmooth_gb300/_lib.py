@@ -31,6 +31,10 @@ SIGNATURES = {
     "asg_smooth": (_i, [_vp, _vp, _i, _f, _f, _f, _vp, _i, _vp, _i, _i, _vp, _vp, _lp, _dp]),
     "asg_load_particles": (_i, [_vp, _vp, _i, _f, _f]),
     "asg_load_particles_device": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _f, _f]),
+    "asg_load_particles_quantised": (_i, [_vp, _vp, _vp, _vp, _i, _f, _f, _f, _i]),
+    "asg_load_particles_quantised_device": (_i, [_vp, _vp, _vp, _vp, _i, _f, _f, _f, _i]),
+    "asg_smooth_quantised": (_i, [_vp, _vp, _vp, _vp, _i, _f, _f, _f, _i, _f, _vp, _i, _i,
+                                  _vp, _vp, _vp, _vp]),
     "asg_run_neighbor_search": (_i, [_vp]),
     "asg_run_mark_halos": (_i, [_vp, _vp, _i, _lp, _dp]),
     "asg_run_fof": (_i, [_vp, _f, _ip]),

@@ -220,6 +220,33 @@ class Context:
                                      C.byref(mh)))
         return meshes, tot.reshape(-1, 2), nph.value, mh.value
 
+    def smooth_quantised(self, cell: np.ndarray, off: np.ndarray, v: np.ndarray | None,
+                         left: float, right: float, cell_size: float, grid: int, boxsize: float,
+                         ncs, sign: int = -1, meshes=None, rk=None, dens=None):
+        """Mixed-precision form of ``smooth`` (no halo marking): positions as an
+        int32 cell index and uint16 offsets (see ``quantised.quantise``).
+        Returns (rk, dens, meshes, totals) with rk and dens in input order."""
+        cell = np.ascontiguousarray(cell, np.int32)
+        off = np.ascontiguousarray(off, np.uint16)
+        n = len(cell)
+        if off.shape != (n, 3):
+            raise ValueError("off must have shape (n, 3)")
+        if v is not None:
+            v = np.ascontiguousarray(v, np.float32)
+        ncs = [int(nc) for nc in ncs]
+        if meshes is None:
+            meshes = [np.zeros(6 * nc ** 3, np.float32) for nc in ncs]
+        rk = np.zeros(n, np.float32) if rk is None else rk
+        dens = np.zeros(n, np.float32) if dens is None else dens
+        arr = (C.c_void_p * len(ncs))(*[m.ctypes.data for m in meshes])
+        nca = np.asarray(ncs, np.int32)
+        tot = np.zeros(2 * len(ncs), np.float64)
+        self._ok(self.lib.asg_smooth_quantised(self.h, _ptr(cell), _ptr(off), _ptr(v), n, left,
+                                               right, cell_size, int(grid), boxsize, _ptr(nca),
+                                               len(ncs), int(sign), _ptr(rk), _ptr(dens), arr,
+                                               _ptr(tot)))
+        return rk, dens, meshes, tot.reshape(-1, 2)
+
     # ---- staged device-resident interface ------------------------------------------
     def load_particles(self, p: np.ndarray, left: float, right: float):
         _check_particles(p)
@@ -230,6 +257,23 @@ class Context:
         self._ok(self.lib.asg_load_particles_device(self.h, C.c_void_p(x_ptr), C.c_void_p(v_ptr),
                                                     C.c_void_p(dens_ptr), C.c_void_p(igrp_ptr),
                                                     int(n), left, right))
+
+    def load_particles_quantised(self, cell: np.ndarray, off: np.ndarray, v: np.ndarray | None,
+                                 left: float, right: float, cell_size: float, grid: int):
+        cell = np.ascontiguousarray(cell, np.int32)
+        off = np.ascontiguousarray(off, np.uint16)
+        if off.shape != (len(cell), 3):
+            raise ValueError("off must have shape (n, 3)")
+        if v is not None:
+            v = np.ascontiguousarray(v, np.float32)
+        self._ok(self.lib.asg_load_particles_quantised(self.h, _ptr(cell), _ptr(off), _ptr(v),
+                                                       len(cell), left, right, cell_size, int(grid)))
+
+    def load_particles_quantised_device(self, cell_ptr: int, off_ptr: int, n: int, left: float,
+                                        right: float, cell_size: float, grid: int, v_ptr: int = 0):
+        self._ok(self.lib.asg_load_particles_quantised_device(
+            self.h, C.c_void_p(cell_ptr), C.c_void_p(off_ptr), C.c_void_p(v_ptr), int(n), left,
+            right, cell_size, int(grid)))
 
     def run_neighbor_search(self):
         self._ok(self.lib.asg_run_neighbor_search(self.h))

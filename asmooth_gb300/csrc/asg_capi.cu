@@ -124,6 +124,7 @@ int device_status(int bits)
     if (bits & ERR_TIES) return ASG_ERR_TIES;
     if (bits & ERR_RANGE) return ASG_ERR_RANGE;
     if (bits & ERR_UF) return ASG_ERR_UNIONFIND;
+    if (bits & ERR_BADCELL) return ASG_ERR_ARG;
     return ASG_OK;
 }
 
@@ -251,6 +252,49 @@ int check_bounds(asg_ctx* ctx, int np, float left, float right)
     if (np <= 0) return fail(ctx, ASG_ERR_ARG, "np must be positive");
     if (!(left < right) || !std::isfinite(left) || !std::isfinite(right))
         return fail(ctx, ASG_ERR_ARG, "need finite left < right");
+    return 0;
+}
+
+int check_quant(asg_ctx* ctx, int grid, float cell_size, float left, float right)
+{
+    if (grid <= 0 || grid > 1290 || !(cell_size > 0.0f) || !std::isfinite(cell_size))
+        return fail(ctx, ASG_ERR_ARG, "quantisation grid: need 0 < grid <= 1290, cell_size > 0");
+    if (!(left + cell_size * (float)grid >= right))
+        return fail(ctx, ASG_ERR_ARG, "quantisation grid does not cover [left, right)");
+    return 0;
+}
+
+// decode mixed-precision positions already on the device and build the index
+void load_quant_device(asg_ctx* ctx, const int* d_cell, const uint16_t* d_off, const float* d_v,
+                       int np, float left, float right, float cell_size, int grid)
+{
+    ctx->n = np;
+    ctx->left = left;
+    ctx->right = right;
+    phase_begin(ctx, ASG_PH_INDEX);
+    launch_unpack_quant(d_cell, d_off, d_v, np, grid, left, cell_size, P<float4>(ctx->pos_in),
+                        P<float4>(ctx->vel_in), P<int>(ctx->igrp_in), P<float>(ctx->rk_in),
+                        ctx->d_err, ctx->s);
+    launch_morton(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
+                  P<int>(ctx->vals0), ctx->s);
+    build_index(ctx);
+}
+
+// host mixed-precision arrays -> one staging buffer [cell | off (16-B padded) | v]
+int stage_quant(asg_ctx* ctx, const int* cell, const uint16_t* off, const float* v, int np,
+                const int** d_cell, const uint16_t** d_off, const float** d_v)
+{
+    const size_t n = (size_t)np;
+    const size_t o_off = (4 * n + 15) & ~size_t(15);
+    const size_t o_v = (o_off + 6 * n + 15) & ~size_t(15);
+    if (int r = grow(ctx, ctx->aos, o_v + (v ? 12 * n : 0))) return r;
+    unsigned char* b = P<unsigned char>(ctx->aos);
+    CK(cudaMemcpyAsync(b, cell, 4 * n, cudaMemcpyHostToDevice, ctx->s));
+    CK(cudaMemcpyAsync(b + o_off, off, 6 * n, cudaMemcpyHostToDevice, ctx->s));
+    if (v) CK(cudaMemcpyAsync(b + o_v, v, 12 * n, cudaMemcpyHostToDevice, ctx->s));
+    *d_cell = reinterpret_cast<const int*>(b);
+    *d_off = reinterpret_cast<const uint16_t*>(b + o_off);
+    *d_v = v ? reinterpret_cast<const float*>(b + o_v) : nullptr;
     return 0;
 }
 
@@ -395,6 +439,40 @@ int asg_load_particles_device(asg_ctx* ctx, const float* d_x, const float* d_v,
                   P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
     int r = finish(ctx, "load_device");
+    if (r) ctx->loaded = false;
+    return r;
+}
+
+int asg_load_particles_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off,
+                                 const float* v, int np, float left, float right, float cell_size,
+                                 int grid)
+{
+    if (!ctx || !cell || !off) return fail(ctx, ASG_ERR_ARG, "null argument");
+    if (int r = check_bounds(ctx, np, left, right)) return r;
+    if (int r = check_quant(ctx, grid, cell_size, left, right)) return r;
+    CK(cudaSetDevice(ctx->device));
+    if (int r = alloc_set(ctx, np)) return r;
+    const int* dc = nullptr;
+    const uint16_t* doff = nullptr;
+    const float* dv = nullptr;
+    if (int r = stage_quant(ctx, cell, off, v, np, &dc, &doff, &dv)) return r;
+    load_quant_device(ctx, dc, doff, dv, np, left, right, cell_size, grid);
+    int r = finish(ctx, "load_quantised");
+    if (r) ctx->loaded = false;
+    return r;
+}
+
+int asg_load_particles_quantised_device(asg_ctx* ctx, const int* d_cell, const uint16_t* d_off,
+                                        const float* d_v, int np, float left, float right,
+                                        float cell_size, int grid)
+{
+    if (!ctx || !d_cell || !d_off) return fail(ctx, ASG_ERR_ARG, "null argument");
+    if (int r = check_bounds(ctx, np, left, right)) return r;
+    if (int r = check_quant(ctx, grid, cell_size, left, right)) return r;
+    CK(cudaSetDevice(ctx->device));
+    if (int r = alloc_set(ctx, np)) return r;
+    load_quant_device(ctx, d_cell, d_off, d_v, np, left, right, cell_size, grid);
+    int r = finish(ctx, "load_quantised_device");
     if (r) ctx->loaded = false;
     return r;
 }
@@ -946,6 +1024,44 @@ int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, f
         CK(cudaMemcpyAsync(totals, ctx->totals.p, 16 * (size_t)n_nc, cudaMemcpyDeviceToHost, ctx->s));
     if (int r = finish(ctx, "smooth")) return r;
     return collect_mark(ctx, nh, np_halo, m_halo);
+}
+
+int asg_smooth_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off, const float* v,
+                         int np, float left, float right, float cell_size, int grid, float boxsize,
+                         const int* ncs, int n_nc, int sign, float* rk, float* dens,
+                         float* const* meshes, double* totals)
+{
+    if (!ctx || !cell || !off) return fail(ctx, ASG_ERR_ARG, "null argument");
+    if (np < K_NN) return fail(ctx, np > 0 ? ASG_ERR_FEW : ASG_ERR_ARG, "fewer than 33 particles");
+    if (int r = check_bounds(ctx, np, left, right)) return r;
+    if (int r = check_quant(ctx, grid, cell_size, left, right)) return r;
+    CK(cudaSetDevice(ctx->device));
+    if (int r = alloc_set(ctx, np)) return r;
+    const size_t n = (size_t)np;
+    if (int r = grow(ctx, ctx->uf, 4 * n)) return r;
+    if (int r = grow(ctx, ctx->minin, 4 * n)) return r;
+    if (int r = grow(ctx, ctx->lab_scan, 4 * n)) return r;
+    const int* dc = nullptr;
+    const uint16_t* doff = nullptr;
+    const float* dv = nullptr;
+    if (int r = stage_quant(ctx, cell, off, v, np, &dc, &doff, &dv)) return r;
+    load_quant_device(ctx, dc, doff, dv, np, left, right, cell_size, grid);
+    run_knn(ctx);
+    if (int r = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0)) return r;
+    // rk and dens back to input order; the particle arrays return in the same call
+    k_dens_of<<<(np + 255) / 256, 256, 0, ctx->s>>>(P<float4>(ctx->vel), np, P<float>(ctx->lab_scan));
+    count_launches(1);
+    launch_scatter_fields(ctx->perm, P<float>(ctx->rk), P<float>(ctx->lab_scan), nullptr, np,
+                          P<float>(ctx->uf), P<float>(ctx->minin), nullptr, ctx->s);
+    if (rk) CK(cudaMemcpyAsync(rk, ctx->uf.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
+    if (dens) CK(cudaMemcpyAsync(dens, ctx->minin.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
+    for (int k = 0; k < n_nc; ++k)
+        if (meshes && meshes[k])
+            CK(cudaMemcpyAsync(meshes[k], ctx->meshes[(size_t)k].mesh.p,
+                               4 * ctx->meshes[(size_t)k].words, cudaMemcpyDeviceToHost, ctx->s));
+    if (totals)
+        CK(cudaMemcpyAsync(totals, ctx->totals.p, 16 * (size_t)n_nc, cudaMemcpyDeviceToHost, ctx->s));
+    return finish(ctx, "smooth_quantised");
 }
 
 }  // extern "C"

@@ -25,6 +25,7 @@ constexpr int ERR_TIES = 8;        // more than TIE_MAX exact ties at the 33rd n
 constexpr int ERR_NONFINITE = 16;  // NaN / inf position
 constexpr int ERR_UF = 32;         // union-find retry limit hit
 constexpr int ERR_RANGE = 64;      // periodic deposit range wider than the mesh
+constexpr int ERR_BADCELL = 128;   // mixed-precision cell index outside the grid
 
 // ---- exact float helpers (reference expression order) ----------------------
 

@@ -54,6 +54,49 @@ __global__ void k_unpack_soa(const float* __restrict__ x3, const float* __restri
     rkin[i] = 0.0f;
 }
 
+// Mixed-precision input: one int32 cell index c = (cz * grid + cy) * grid + cx
+// and three uint16 offsets per particle.  Each coordinate decodes as
+//   x = (left + cs * cx) + off * unit,   unit = cs / 65536,
+// every product and sum rounded to nearest in this order (the host decode in
+// the Python package does the same float32 operations).
+__global__ void k_unpack_quant(const int* __restrict__ cell, const uint16_t* __restrict__ off,
+                               const float* __restrict__ v3, int n, int grid, float left, float cs,
+                               float unit, float4* __restrict__ pos, float4* __restrict__ vel,
+                               int* __restrict__ igrp, float* __restrict__ rkin, int* err)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = cell[i];
+    const int g2 = grid * grid;
+    if (c < 0 || (long long)c >= (long long)g2 * grid) {
+        atomicOr(err, ERR_BADCELL);
+        c = 0;
+    }
+    const int cx = c % grid, cy = (c / grid) % grid, cz = c / g2;
+    const float x = __fadd_rn(__fadd_rn(left, __fmul_rn(cs, (float)cx)),
+                              __fmul_rn((float)off[3 * (size_t)i], unit));
+    const float y = __fadd_rn(__fadd_rn(left, __fmul_rn(cs, (float)cy)),
+                              __fmul_rn((float)off[3 * (size_t)i + 1], unit));
+    const float z = __fadd_rn(__fadd_rn(left, __fmul_rn(cs, (float)cz)),
+                              __fmul_rn((float)off[3 * (size_t)i + 2], unit));
+    pos[i] = make_float4(x, y, z, __int_as_float(i));
+    vel[i] = v3 ? make_float4(v3[3 * (size_t)i], v3[3 * (size_t)i + 1], v3[3 * (size_t)i + 2], 0.0f)
+                : make_float4(0.f, 0.f, 0.f, 0.f);
+    igrp[i] = 0;
+    rkin[i] = 0.0f;
+}
+
+void launch_unpack_quant(const int* cell, const uint16_t* off, const float* v, int n, int grid,
+                         float left, float cs, float4* pos_in, float4* vel_in, int* igrp_in,
+                         float* rk_in, int* err, cudaStream_t s)
+{
+    if (n <= 0) return;
+    const float unit = cs / 65536.0f;
+    k_unpack_quant<<<(n + 255) / 256, 256, 0, s>>>(cell, off, v, n, grid, left, cs, unit, pos_in,
+                                                    vel_in, igrp_in, rk_in, err);
+    count_launches(1);
+}
+
 void launch_unpack_aos(const void* aos, int n, float4* pos_in, float4* vel_in, int* igrp_in,
                        float* rk_in, int* err, cudaStream_t s)
 {

@@ -42,6 +42,10 @@ void launch_unpack_aos(const void* aos, int n, float4* pos_in, float4* vel_in, i
 void launch_unpack_soa(const float* x, const float* v, const float* dens, const int* igrp, int n,
                        float4* pos_in, float4* vel_in, int* igrp_in, float* rk_in, int* err,
                        cudaStream_t s);
+// mixed-precision positions: int32 cell index + 3 x uint16 offsets in cells of side cs
+void launch_unpack_quant(const int* cell, const uint16_t* off, const float* v, int n, int grid,
+                         float left, float cs, float4* pos_in, float4* vel_in, int* igrp_in,
+                         float* rk_in, int* err, cudaStream_t s);
 // 48-bit Morton keys (16 bits per axis) over [left, right)^3, or over the
 // particles' own bounding cube when d_lohi (2 ints of scratch) is given;
 // key_prefix lands in bits 48+ (batched cubes)

@@ -195,13 +195,12 @@ def add_periodic_shell(x: np.ndarray, v: np.ndarray, boxsize: float,
                 n_local, float(boxsize), float(dx))
 
 
-def quantise_positions(x: np.ndarray, left: float, cell: float = 4.0):
-    """Mixed-precision layout: int32 cell index per axis packed into one int32
-    plus uint16 offsets within ``cell``-unit cells (resolution cell/65536)."""
-    rel = (x.astype(np.float64) - left) / cell
-    ci = np.floor(rel).astype(np.int64)
-    off = np.clip(np.floor((rel - ci) * 65536.0), 0, 65535).astype(np.uint16)
-    return ci.astype(np.int32), off
+def quantise_positions(cube: Cube, cell_size: float = 4.0):
+    """Mixed-precision form of a cube's positions (4-unit cells, 16-bit
+    offsets): returns (cell, off, grid) as ``quantised.quantise``."""
+    from .quantised import quantise
+
+    return quantise(cube.x, cube.left, cube.right, cell_size)
 
 
 def write_xv(path: str, x: np.ndarray, v: np.ndarray) -> None:

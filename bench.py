@@ -42,6 +42,24 @@ def env_int(k, d):
         return d
 
 
+def max_over_ranks(x: float, dist=None, device: str = "cuda") -> float:
+    """The largest of every rank's x (the job's time is its slowest replica);
+    x itself when not distributed."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(n_local: int, world: int, seconds: float) -> float:
+    """Whole-job particles/s of `world` independent replica cubes of n_local
+    particles each, all finished within `seconds` (the max over ranks)."""
+    return world * n_local / seconds
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -211,41 +229,44 @@ def run_ours(args):
         ctx.run_neighbor_search()
         ctx.run_deposit(cube.boxsize, ncs, sign=-1)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    ctx.set_timing(True)
-    clocks = ClockSampler(local)
-    clocks.start()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    launches0 = ctx.kernel_launches
-    total_ms = 0.0
-    wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.zero_()  # L2 flush between timed steps (not timed)
+    def timed(step_fn, sample_clocks):
+        """W warm-up steps, then K steps each timed with CUDA events on the
+        context stream, L2 flushed before each; max over ranks."""
+        for _ in range(args.warmup):
+            step_fn()
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        step()
-        e1.record(stream)
-        e1.synchronize()
-        total_ms += e0.elapsed_time(e1)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    wall = time.perf_counter() - wall0
-    launches = ctx.kernel_launches - launches0
-    phases = ctx.phase_ms()
-    ctx.set_timing(False)
-    clk = clocks.stop()
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_step = float(t.item()) / args.steps
-    value = world * n_local / (ms_step * 1e-3)
+        ctx.set_timing(True)
+        clocks = ClockSampler(local) if sample_clocks else None
+        if clocks:
+            clocks.start()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        launches0 = ctx.kernel_launches
+        total_ms = 0.0
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (not timed)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step_fn()
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        wall = time.perf_counter() - wall0
+        launches = ctx.kernel_launches - launches0
+        phases = ctx.phase_ms()
+        ctx.set_timing(False)
+        clk = clocks.stop() if clocks else None
+        return max_over_ranks(total_ms, dist) / args.steps, phases, launches, clk, wall
+
+    ms_step, phases, launches, clk, wall = timed(step, True)
+    value = replica_value(n_local, world, ms_step * 1e-3)
 
     # end to end through the public C ABI: pinned host Particle records in, out
     rec_bytes = n * api.PARTICLE_DTYPE.itemsize
@@ -266,10 +287,8 @@ def run_ours(args):
             w0 = time.perf_counter()
             ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
             e2e_times.append(time.perf_counter() - w0)
-        tt = torch.tensor([statistics.mean(e2e_times)], dtype=torch.float64, device="cuda")
-        if dist:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e = {"value": world * n_local / float(tt.item()), "unit": "particles/s",
+        tt = max_over_ranks(statistics.mean(e2e_times), dist)
+        e2e = {"value": replica_value(n_local, world, tt), "unit": "particles/s",
                "h2d_bytes_per_step": rec_bytes, "d2h_bytes_per_step": d2h}
         rk_host = p["rk"].copy()
     else:
@@ -310,6 +329,61 @@ def run_ours(args):
             "step_hbm_gbs_vs_peak": {"achieved": hbm_alg / (ms_step * 1e-3) / 1e9,
                                      "peak": pk["hbm_gbs"], "peak_kind": pk_kind}}
 
+    # mixed-precision form: positions as int32 cell index + uint16 offsets in
+    # 4-unit cells, decoded on the device, then the same FP32 path
+    mixed = None
+    if not args.no_mixed:
+        cell, off, grid = syn.quantise_positions(cube)
+        cell_d = torch.from_numpy(cell).cuda()
+        off_d = torch.from_numpy(off.view(np.int16)).cuda()
+
+        def step_mixed():
+            ctx.load_particles_quantised_device(cell_d.data_ptr(), off_d.data_ptr(), n, cube.left,
+                                                cube.right, 4.0, grid, v_ptr=v_d.data_ptr())
+            ctx.run_neighbor_search()
+            ctx.run_deposit(cube.boxsize, ncs, sign=-1)
+
+        ms_m, phases_m, launches_m, _, _ = timed(step_mixed, False)
+        rkm_d = torch.empty(n, dtype=torch.float32, device="cuda")
+        ctx.store_fields_device(rk_ptr=rkm_d.data_ptr())
+        rel = np.abs(rkm_d.cpu().numpy().astype(np.float64) - rk_host) / rk_host
+        mixed = {"value": replica_value(n_local, world, ms_m * 1e-3), "unit": "particles/s",
+                 "ms_per_step": ms_m, "vs_plain": ms_step / ms_m, "gpu_launches": launches_m,
+                 "phase_ms_per_step": {k: v / args.steps for k, v in phases_m.items()},
+                 "input": "int32 cell index + 3 x uint16 offsets (4-unit cells) + float32 v",
+                 "h_rel_err_vs_fp32_positions": {"max": float(rel.max()),
+                                                 "median": float(np.median(rel))}}
+        if not args.no_e2e:
+            def pinned(shape, dt):
+                return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+
+            cell_h = pinned(n, torch.int32)
+            cell_h[:] = cell
+            off_h = pinned((n, 3), torch.int16).view(np.uint16)
+            off_h[:] = off
+            v_h = pinned((n, 3), torch.float32)
+            v_h[:] = cube.v
+            rk_o, dens_o = pinned(n, torch.float32), pinned(n, torch.float32)
+            mesh_q = [pinned(6 * nc ** 3, torch.float32) for nc in ncs]
+
+            def call():
+                ctx.smooth_quantised(cell_h, off_h, v_h, cube.left, cube.right, 4.0, grid,
+                                     cube.boxsize, ncs, -1, meshes=mesh_q, rk=rk_o, dens=dens_o)
+
+            for _ in range(max(1, args.warmup)):
+                call()
+            times = []
+            for _ in range(args.steps):
+                torch.cuda.synchronize()
+                w0 = time.perf_counter()
+                call()
+                times.append(time.perf_counter() - w0)
+            tt = max_over_ranks(statistics.mean(times), dist)
+            mixed["e2e"] = {"value": replica_value(n_local, world, tt), "unit": "particles/s",
+                            "h2d_bytes_per_step": 22 * n,
+                            "d2h_bytes_per_step": 8 * n + sum(4 * 6 * nc ** 3 for nc in ncs)
+                            + 16 * len(ncs)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -336,6 +410,8 @@ def run_ours(args):
         "clocks": clk,
         "wall_s_timed": wall,
     }
+    if mixed:
+        line["mixed"] = mixed
     if cpu:
         line["cpu_baseline"] = cpu
     if rank == 0:
@@ -354,6 +430,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg2_s2"],
                     help="cfg2_s2: the same model at 1/8 volume, for profiling captures")
     args = ap.parse_args()

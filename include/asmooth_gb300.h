@@ -18,6 +18,8 @@
 #ifndef ASMOOTH_GB300_H
 #define ASMOOTH_GB300_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -151,6 +153,31 @@ int asg_store_fields_device(asg_ctx* ctx, float* d_rk, float* d_dens, int* d_igr
 /* Neighbour-search internals in input order (host arrays, any may be NULL):
  * t33 = d2 of the 33rd key, idx33 = its input index. */
 int asg_get_knn(asg_ctx* ctx, float* t33, int* idx33);
+
+/* ---- mixed-precision form ---------------------------------------------------------
+ * No counterpart in the reference, whose positions are always float x[3]:
+ * positions arrive as one int32 cell index c = (cz*grid + cy)*grid + cx of a
+ * cubic grid of side cell_size starting at left, plus three uint16 offsets
+ * (np*3, xyz interleaved) in units of cell_size/65536.  The device decodes
+ *   x = (left + cell_size*cx) + off_x*(cell_size/65536)
+ * with every product and sum rounded to nearest float in this order, then runs
+ * the same FP32 path as the plain form, so the results equal the plain form's
+ * on the decoded positions.  grid*cell_size must cover [left, right); a cell
+ * index outside [0, grid^3) returns ASG_ERR_ARG.  v (np*3) may be NULL. */
+int asg_load_particles_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off,
+                                 const float* v, int np, float left, float right, float cell_size,
+                                 int grid);
+int asg_load_particles_quantised_device(asg_ctx* ctx, const int* d_cell, const uint16_t* d_off,
+                                        const float* d_v, int np, float left, float right,
+                                        float cell_size, int grid);
+/* One-shot form of asg_smooth for mixed-precision input (no halo marking):
+ * rk and dens (host, np each, input order, may be NULL) receive the smoothing
+ * length and the particle density; meshes and totals as in asg_smooth. */
+int asg_smooth_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off, const float* v,
+                         int np, float left, float right, float cell_size, int grid, float boxsize,
+                         const int* ncs, int n_nc, int sign, float* rk, float* dens,
+                         float* const* meshes, double* totals);
+
 /* CUDA stream used by the context (cudaStream_t as void*). */
 void* asg_stream(asg_ctx* ctx);
 /* Count of kernels this library has launched so far (process-wide). */
