@@ -29,6 +29,20 @@ SIGNATURES = {
     "asg_remove_small_groups": (_i, [_vp, _vp, _i, _i, _ip]),
     "asg_mark_halo_particles": (_i, [_vp, _vp, _i, _vp, _i, _f, _f, _lp, _dp]),
     "asg_smooth": (_i, [_vp, _vp, _i, _f, _f, _f, _vp, _i, _vp, _i, _i, _vp, _vp, _lp, _dp]),
+    "asg_write_mesh_separate": (_i, [_vp, C.c_char_p, _i, _vp, _i, _f]),
+    "asg_write_mesh_device": (_i, [_vp, _i, C.c_char_p, _i]),
+    "asg_write_mesh": (_i, [C.c_char_p, _vp, _i, _f]),
+    "asg_fof_halos": (_i, [_vp, _vp, _i, _i, _f, _vp, _ip]),
+    "asg_write_fof_halos": (_i, [_vp, C.c_char_p, _vp, _i, _i, _f]),
+    "asg_run_fof_halos": (_i, [_vp, _i, _f, _vp, _ip]),
+    "asg_load_periodic_cube": (_i, [_vp, _vp, _i, _f, _f, _ip, _ip]),
+    "asg_load_periodic_cube_device": (_i, [_vp, _vp, _vp, _i, _f, _f, _ip, _ip]),
+    "asg_decode_xv": (_i, [_vp, _vp, _i, _vp]),
+    "asg_decode_zip": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _f, _vp]),
+    "asg_read_pm_file_xv": (_i, [_vp, C.c_char_p, C.c_char_p, _i, _vp, _ip]),
+    "asg_read_pm_file_zip": (_i, [_vp, C.c_char_p, C.c_char_p, _i, _i, _i, _vp, _ip, _fp]),
+    "asg_copy_decoded": (_i, [_vp, _vp]),
+    "asg_load_decoded_periodic": (_i, [_vp, _f, _f, _ip, _ip]),
     "asg_load_particles": (_i, [_vp, _vp, _i, _f, _f]),
     "asg_load_particles_device": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _f, _f]),
     "asg_load_particles_quantised": (_i, [_vp, _vp, _vp, _vp, _i, _f, _f, _f, _i]),

@@ -15,6 +15,8 @@ reference's names and argument meaning:
   normalise_mesh         write_mesh_separate normalisation (coarse_mesh.cpp:158-171)
   group_fof, remove_small_groups (fof.cpp:34-166)
   mark_halo_particles    SO-halo loop (clumping_tree_main.cpp:465-485)
+  write_mesh_separate, write_mesh (coarse_mesh.cpp:128-208)
+  write_fof_halos        FOF catalogue file (fof.cpp:169-219)
 
 Where the reference asserts or aborts, these raise :class:`AsmoothError`.
 """
@@ -29,6 +31,9 @@ from . import _lib
 PARTICLE_DTYPE = np.dtype([("x", "<f4", (3,)), ("v", "<f4", (3,)), ("dens", "<f4"),
                            ("rk", "<f4"), ("igrp", "<i4")])
 HALO_DTYPE = np.dtype([("x", "<f4", (3,)), ("r", "<f4"), ("mass", "<f4")])
+# struct FofHalo (fof.cpp:22-25), the record of the FOF catalogue file
+FOF_HALO_DTYPE = np.dtype([("x", "<f4", (3,)), ("v", "<f4", (3,)), ("nfof", "<i4")])
+assert FOF_HALO_DTYPE.itemsize == 28
 assert PARTICLE_DTYPE.itemsize == 36 and HALO_DTYPE.itemsize == 20
 
 ASG_OK = 0
@@ -36,6 +41,7 @@ ASG_ERR_ARG, ASG_ERR_CUDA, ASG_ERR_NOMEM, ASG_ERR_FEW, ASG_ERR_ZERO_RK = -1, -2,
 ASG_ERR_NONFINITE, ASG_ERR_STACK, ASG_ERR_TIES, ASG_ERR_RANGE, ASG_ERR_STATE = -6, -7, -8, -9, -10
 ASG_ERR_UNIONFIND = -11
 ASG_ERR_NOALLOC_LIMIT = -12
+ASG_ERR_IO = -13
 
 
 class AsmoothError(RuntimeError):
@@ -247,6 +253,39 @@ class Context:
                                                _ptr(tot)))
         return rk, dens, meshes, tot.reshape(-1, 2)
 
+    # ---- outputs ----------------------------------------------------------------
+    def write_mesh_separate(self, base: str, inode: int, mesh: np.ndarray, nc: int,
+                            boxsize: float) -> np.ndarray:
+        """write_mesh_separate: normalise ``mesh`` in place, write the four files."""
+        if mesh.dtype != np.float32 or not mesh.flags.c_contiguous or mesh.size != 6 * nc ** 3:
+            raise TypeError("mesh must be a contiguous float32 array of 6*nc^3 values")
+        self._ok(self.lib.asg_write_mesh_separate(self.h, base.encode(), int(inode), _ptr(mesh),
+                                                  int(nc), boxsize))
+        return mesh
+
+    def write_mesh_device(self, k: int, base: str, inode: int):
+        self._ok(self.lib.asg_write_mesh_device(self.h, int(k), base.encode(), int(inode)))
+
+    def fof_halos(self, p: np.ndarray, nhalo: int, boxsize: float) -> np.ndarray:
+        """write_fof_halos' catalogue (records of FOF_HALO_DTYPE) of labels 1..nhalo."""
+        _check_particles(p)
+        out = np.zeros(max(int(nhalo), 1), FOF_HALO_DTYPE)
+        nl = C.c_int(0)
+        self._ok(self.lib.asg_fof_halos(self.h, _ptr(p), len(p), int(nhalo), boxsize, _ptr(out),
+                                        C.byref(nl)))
+        return out[:nl.value].copy()
+
+    def write_fof_halos(self, filename: str, p: np.ndarray, nhalo: int, boxsize: float):
+        _check_particles(p)
+        self._ok(self.lib.asg_write_fof_halos(self.h, filename.encode(), _ptr(p), len(p),
+                                              int(nhalo), boxsize))
+
+    def run_fof_halos(self, nhalo: int, boxsize: float) -> np.ndarray:
+        out = np.zeros(max(int(nhalo), 1), FOF_HALO_DTYPE)
+        nl = C.c_int(0)
+        self._ok(self.lib.asg_run_fof_halos(self.h, int(nhalo), boxsize, _ptr(out), C.byref(nl)))
+        return out[:nl.value].copy()
+
     # ---- staged device-resident interface ------------------------------------------
     def load_particles(self, p: np.ndarray, left: float, right: float):
         _check_particles(p)
@@ -257,6 +296,74 @@ class Context:
         self._ok(self.lib.asg_load_particles_device(self.h, C.c_void_p(x_ptr), C.c_void_p(v_ptr),
                                                     C.c_void_p(dens_ptr), C.c_void_p(igrp_ptr),
                                                     int(n), left, right))
+
+    def load_periodic_cube(self, p: np.ndarray, boxsize: float, buffer_factor: float):
+        """The whole box plus its periodic buffer shell built on the device
+        (one-rank exchange_buffer + remove_extra_particles); returns
+        (np_with_buffers, np_local_kept).  store_particles reads the set back."""
+        _check_particles(p)
+        nw, nl = C.c_int(0), C.c_int(0)
+        self._ok(self.lib.asg_load_periodic_cube(self.h, _ptr(p), len(p), boxsize, buffer_factor,
+                                                 C.byref(nw), C.byref(nl)))
+        return nw.value, nl.value
+
+    def load_periodic_cube_device(self, x_ptr: int, n: int, boxsize: float, buffer_factor: float,
+                                  v_ptr: int = 0):
+        nw, nl = C.c_int(0), C.c_int(0)
+        self._ok(self.lib.asg_load_periodic_cube_device(self.h, C.c_void_p(x_ptr), C.c_void_p(v_ptr),
+                                                        int(n), boxsize, buffer_factor,
+                                                        C.byref(nw), C.byref(nl)))
+        return nw.value, nl.value
+
+    # ---- particle files decoded on the device ---------------------------------------
+    def decode_xv(self, xv: np.ndarray, shift=(0.0, 0.0, 0.0)) -> int:
+        """xv payload (n, 6) float32 -> decoded particles kept on the device."""
+        xv = np.ascontiguousarray(xv, np.float32).reshape(-1, 6)
+        sh = np.asarray(shift, np.float32)
+        self._ok(self.lib.asg_decode_xv(self.h, _ptr(xv), len(xv), _ptr(sh)))
+        return len(xv)
+
+    def decode_zip(self, zip0: np.ndarray, zip1: np.ndarray, zip2: np.ndarray, zip3: np.ndarray,
+                   np_local: int, nc_node_dim: int, mesh_scale: int, v_r2i: float,
+                   shift=(0.0, 0.0, 0.0)) -> int:
+        z0 = np.ascontiguousarray(zip0, np.uint8)
+        z1 = np.ascontiguousarray(zip1, np.int16)
+        z2 = np.ascontiguousarray(zip2, np.uint8)
+        z3 = np.ascontiguousarray(zip3, np.int32)
+        sh = np.asarray(shift, np.float32)
+        self._ok(self.lib.asg_decode_zip(self.h, _ptr(z0), _ptr(z1), _ptr(z2), _ptr(z3), z3.size,
+                                         int(np_local), int(nc_node_dim), int(mesh_scale),
+                                         float(v_r2i), _ptr(sh)))
+        return int(np_local)
+
+    def read_pm_file_xv(self, filebase: str, redshift: str, inode: int,
+                        shift=(0.0, 0.0, 0.0)) -> int:
+        sh = np.asarray(shift, np.float32)
+        n = C.c_int(0)
+        self._ok(self.lib.asg_read_pm_file_xv(self.h, filebase.encode(), redshift.encode(),
+                                              int(inode), _ptr(sh), C.byref(n)))
+        return n.value
+
+    def read_pm_file_zip(self, filebase: str, redshift: str, inode: int, nc_node_dim: int,
+                         mesh_scale: int, shift=(0.0, 0.0, 0.0)):
+        """Returns (np_local, boxsize); the particles stay on the device."""
+        sh = np.asarray(shift, np.float32)
+        n, L = C.c_int(0), C.c_float(0.0)
+        self._ok(self.lib.asg_read_pm_file_zip(self.h, filebase.encode(), redshift.encode(),
+                                               int(inode), int(nc_node_dim), int(mesh_scale),
+                                               _ptr(sh), C.byref(n), C.byref(L)))
+        return n.value, L.value
+
+    def copy_decoded(self, n: int) -> np.ndarray:
+        out = np.zeros(int(n), PARTICLE_DTYPE)
+        self._ok(self.lib.asg_copy_decoded(self.h, _ptr(out)))
+        return out
+
+    def load_decoded_periodic(self, boxsize: float, buffer_factor: float):
+        nw, nl = C.c_int(0), C.c_int(0)
+        self._ok(self.lib.asg_load_decoded_periodic(self.h, boxsize, buffer_factor, C.byref(nw),
+                                                    C.byref(nl)))
+        return nw.value, nl.value
 
     def load_particles_quantised(self, cell: np.ndarray, off: np.ndarray, v: np.ndarray | None,
                                  left: float, right: float, cell_size: float, grid: int):
@@ -380,3 +487,21 @@ def remove_small_groups(p, ngrp):
 
 def mark_halo_particles(p, halos, left, right):
     return default_context().mark_halo_particles(p, halos, left, right)
+
+
+def write_mesh_separate(base, inode, mesh, nc, boxsize):
+    return default_context().write_mesh_separate(base, inode, mesh, nc, boxsize)
+
+
+def write_mesh(filename, mesh, nc, boxsize):
+    """write_mesh (coarse_mesh.cpp:128-143); host only, needs no GPU."""
+    m = np.ascontiguousarray(mesh, np.float32)
+    if m.size != 6 * nc ** 3:
+        raise ValueError("mesh must hold 6*nc^3 floats")
+    rc = _lib.load().asg_write_mesh(filename.encode(), _ptr(m), int(nc), float(boxsize))
+    if rc:
+        raise AsmoothError(rc, f"write_mesh {filename}")
+
+
+def write_fof_halos(filename, p, nhalo, boxsize):
+    return default_context().write_fof_halos(filename, p, nhalo, boxsize)

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libasmooth_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-UNITS = ["asg_index", "asg_knn", "asg_deposit", "asg_fof", "asg_capi", "asg_noalloc"]
+UNITS = ["asg_index", "asg_knn", "asg_deposit", "asg_fof", "asg_output", "asg_shell", "asg_decode", "asg_capi", "asg_noalloc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 

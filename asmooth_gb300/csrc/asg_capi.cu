@@ -5,6 +5,7 @@
 // its kernels on the context stream, synchronises once at the end and turns
 // the device error word into a status code.
 #include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -60,6 +61,10 @@ struct asg_ctx {
     Buf halos, hcount, hmass;
     Buf totals, lohi;
     Buf dep_rec, dep_pcount, dep_tiles, dep_counter, dep_pairs, dep_sort, dep_partial;
+    Buf cat, cat_out;  // FOF catalogue scratch and records
+    Buf sh_in, sh_all; // periodic shell: interior input + bin sort, all copies + flags
+    Buf dec_raw, dec_scan;  // file payloads on the device, zip count scans
+    int dec_n = 0;          // particles of the last decode (in sh_in), 0 = none
     uint32_t dep_npairs = 0;
     int dep_tiles_n = 0;
     uint32_t* h_u32 = nullptr;  // pinned
@@ -333,6 +338,7 @@ const char* asg_strerror(int status)
     case ASG_ERR_STATE: return "call order: a required previous step is missing";
     case ASG_ERR_UNIONFIND: return "union-find retry limit reached";
     case ASG_ERR_NOALLOC_LIMIT: return "input larger than the allocation-free entry point's scratch";
+    case ASG_ERR_IO: return "output file could not be opened or written";
     default: return "unknown status";
     }
 }
@@ -378,7 +384,8 @@ void asg_destroy(asg_ctx* ctx)
                    &ctx->scan_tmp, &ctx->lab_cnt, &ctx->lab_scan, &ctx->halos, &ctx->hcount,
                    &ctx->hmass, &ctx->totals, &ctx->lohi, &ctx->dep_rec, &ctx->dep_pcount,
                    &ctx->dep_tiles, &ctx->dep_counter, &ctx->dep_pairs, &ctx->dep_sort,
-                   &ctx->dep_partial};
+                   &ctx->dep_partial, &ctx->cat, &ctx->cat_out, &ctx->sh_in, &ctx->sh_all,
+                   &ctx->dec_raw, &ctx->dec_scan};
     for (Buf* b : bufs)
         if (b->p) cudaFree(b->p);
     for (auto& m : ctx->meshes) {
@@ -395,6 +402,113 @@ void asg_destroy(asg_ctx* ctx)
 
 void* asg_stream(asg_ctx* ctx) { return ctx ? (void*)ctx->s : nullptr; }
 long long asg_kernel_launches(asg_ctx*) { return g_launches.load(); }
+
+// ---- periodic shell of a single-cube run ----------------------------------------------
+
+struct ShellIn {  // interior particles + bin sort scratch inside ctx->sh_in
+    size_t pos, vel, igrp, rk, k0, k1, v0, v1, tmp, start, end, total;
+};
+
+static ShellIn shell_in_layout(int n)
+{
+    ShellIn L{};
+    const size_t N = (size_t)n;
+    size_t o = 0;
+    auto take = [&](size_t b) {
+        const size_t at = o;
+        o = (o + b + 255) & ~size_t(255);
+        return at;
+    };
+    L.pos = take(16 * N);
+    L.vel = take(16 * N);
+    L.igrp = take(4 * N);
+    L.rk = take(4 * N);
+    L.k0 = take(4 * N);
+    L.k1 = take(4 * N);
+    L.v0 = take(4 * N);
+    L.v1 = take(4 * N);
+    L.tmp = take(radix_sort_temp_bytes(n));
+    L.start = take(27 * 4);
+    L.end = take(27 * 4);
+    L.total = o;
+    return L;
+}
+
+static int check_shell(asg_ctx* ctx, int np, float boxsize, float bf)
+{
+    if (np <= 0) return fail(ctx, ASG_ERR_ARG, "np must be positive");
+    if (!(boxsize > 0.0f) || !std::isfinite(boxsize) || !(bf > 0.0f) || !(bf < 0.5f))
+        return fail(ctx, ASG_ERR_ARG, "need boxsize > 0 and 0 < buffer_factor < 0.5");
+    return 0;
+}
+
+// sh_in holds the interior particles (unpacked); build the shell and load the set
+static int load_shell(asg_ctx* ctx, int np, float boxsize, float bf, int* np_with, int* np_local)
+{
+    const ShellIn L = shell_in_layout(np);
+    unsigned char* b = P<unsigned char>(ctx->sh_in);
+    auto F4 = [&](size_t o) { return reinterpret_cast<float4*>(b + o); };
+    auto U = [&](size_t o) { return reinterpret_cast<uint32_t*>(b + o); };
+    auto I = [&](size_t o) { return reinterpret_cast<int*>(b + o); };
+    const float lt = bf * boxsize, rt = (1.0f - bf) * boxsize;  // exchange_buffer.cpp:23-24
+    const uint32_t* keys = nullptr;
+    const int* order = nullptr;
+    launch_shell_bins(F4(L.pos), np, lt, rt, U(L.k0), I(L.v0), U(L.k1), I(L.v1), b + L.tmp,
+                      U(L.start), U(L.end), &keys, &order, ctx->s);
+    uint32_t se[54];
+    CK(cudaMemcpyAsync(se, b + L.start, 27 * 4, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(se + 27, b + L.end, 27 * 4, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    // the reference's send loop order (exchange_buffer.cpp:120-150): source bin, then direction
+    ShellPlan plan;
+    size_t off = (size_t)np;
+    for (int i = 0; i < 27; ++i)
+        for (int j = 0; j < 27; ++j) {
+            plan.base[i][j] = -1;
+            if (i == 13 || j == 13) continue;
+            bool send = true;
+            for (int a = 0, bi = i, dj = j; a < 3; ++a, bi /= 3, dj /= 3)
+                send = send && (dj % 3 == 1 || dj % 3 == bi % 3);
+            if (!send) continue;
+            plan.base[i][j] = (int)off;
+            off += se[27 + i] - se[i];
+        }
+    if (off > (size_t)INT_MAX) return fail(ctx, ASG_ERR_ARG, "shell too large for int indices");
+    const int n_all = (int)off;
+    const size_t A = (size_t)n_all;
+    const size_t o_vel = 16 * A, o_igrp = 32 * A, o_rk = 36 * A, o_flags = 40 * A;
+    const size_t o_scan = (o_flags + 4 * (A + 1) + 255) & ~size_t(255);
+    if (int r = grow(ctx, ctx->sh_all, o_scan + scan_temp_bytes(A + 1))) return r;
+    if (int r = alloc_set(ctx, n_all)) return r;  // the kept set is at most n_all
+    unsigned char* a = P<unsigned char>(ctx->sh_all);
+    launch_shell_emit(F4(L.pos), F4(L.vel), I(L.igrp), reinterpret_cast<float*>(b + L.rk), keys,
+                      order, U(L.start), np, plan, boxsize, reinterpret_cast<float4*>(a),
+                      reinterpret_cast<float4*>(a + o_vel), reinterpret_cast<int*>(a + o_igrp),
+                      reinterpret_cast<float*>(a + o_rk), ctx->s);
+    const float dx = bf * boxsize;  // clumping_tree_main.cpp:556-558
+    uint32_t* flags = reinterpret_cast<uint32_t*>(a + o_flags);
+    launch_shell_filter(reinterpret_cast<float4*>(a), reinterpret_cast<float4*>(a + o_vel),
+                        reinterpret_cast<int*>(a + o_igrp), reinterpret_cast<float*>(a + o_rk),
+                        n_all, -dx, boxsize + dx, flags, a + o_scan, P<float4>(ctx->pos_in),
+                        P<float4>(ctx->vel_in), P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->s);
+    CK(cudaMemcpyAsync(ctx->h_u32, flags + n_all, 4, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(ctx->h_u32 + 1, flags + np, 4, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    const int n = (int)ctx->h_u32[0];
+    if (np_with) *np_with = n;
+    if (np_local) *np_local = (int)ctx->h_u32[1];
+    if (n < K_NN) return fail(ctx, ASG_ERR_FEW, "fewer than 33 particles with the shell");
+    ctx->n = n;
+    ctx->left = -dx;
+    ctx->right = boxsize + dx;
+    phase_begin(ctx, ASG_PH_INDEX);
+    launch_morton(P<float4>(ctx->pos_in), n, ctx->left, ctx->right, nullptr, 0,
+                  P<uint64_t>(ctx->keys0), P<int>(ctx->vals0), ctx->s);
+    build_index(ctx);
+    int r = finish(ctx, "load_periodic_cube");
+    if (r) ctx->loaded = false;
+    return r;
+}
 
 // ---- staged interface ---------------------------------------------------------
 
@@ -475,6 +589,196 @@ int asg_load_particles_quantised_device(asg_ctx* ctx, const int* d_cell, const u
     int r = finish(ctx, "load_quantised_device");
     if (r) ctx->loaded = false;
     return r;
+}
+
+int asg_load_periodic_cube(asg_ctx* ctx, const asg_particle* p, int np_local, float boxsize,
+                           float buffer_factor, int* np_with_buffers, int* np_local_kept)
+{
+    if (!ctx || !p) return fail(ctx, ASG_ERR_ARG, "null argument");
+    if (int r = check_shell(ctx, np_local, boxsize, buffer_factor)) return r;
+    CK(cudaSetDevice(ctx->device));
+    ctx->loaded = false;
+    const ShellIn L = shell_in_layout(np_local);
+    if (int r = grow(ctx, ctx->sh_in, L.total)) return r;
+    if (int r = grow(ctx, ctx->aos, sizeof(asg_particle) * (size_t)np_local)) return r;
+    CK(cudaMemcpyAsync(ctx->aos.p, p, sizeof(asg_particle) * (size_t)np_local,
+                       cudaMemcpyHostToDevice, ctx->s));
+    unsigned char* b = P<unsigned char>(ctx->sh_in);
+    launch_unpack_aos(ctx->aos.p, np_local, reinterpret_cast<float4*>(b + L.pos),
+                      reinterpret_cast<float4*>(b + L.vel), reinterpret_cast<int*>(b + L.igrp),
+                      reinterpret_cast<float*>(b + L.rk), ctx->d_err, ctx->s);
+    ctx->dec_n = np_local;  // sh_in now holds these interior particles
+    return load_shell(ctx, np_local, boxsize, buffer_factor, np_with_buffers, np_local_kept);
+}
+
+int asg_load_periodic_cube_device(asg_ctx* ctx, const float* d_x, const float* d_v, int np_local,
+                                  float boxsize, float buffer_factor, int* np_with_buffers,
+                                  int* np_local_kept)
+{
+    if (!ctx || !d_x) return fail(ctx, ASG_ERR_ARG, "null argument");
+    if (int r = check_shell(ctx, np_local, boxsize, buffer_factor)) return r;
+    CK(cudaSetDevice(ctx->device));
+    ctx->loaded = false;
+    const ShellIn L = shell_in_layout(np_local);
+    if (int r = grow(ctx, ctx->sh_in, L.total)) return r;
+    unsigned char* b = P<unsigned char>(ctx->sh_in);
+    launch_unpack_soa(d_x, d_v, nullptr, nullptr, np_local, reinterpret_cast<float4*>(b + L.pos),
+                      reinterpret_cast<float4*>(b + L.vel), reinterpret_cast<int*>(b + L.igrp),
+                      reinterpret_cast<float*>(b + L.rk), ctx->d_err, ctx->s);
+    ctx->dec_n = np_local;  // sh_in now holds these interior particles
+    return load_shell(ctx, np_local, boxsize, buffer_factor, np_with_buffers, np_local_kept);
+}
+
+// ---- particle files decoded on the device ---------------------------------------------
+
+static size_t a16(size_t v) { return (v + 15) & ~size_t(15); }
+
+int asg_decode_xv(asg_ctx* ctx, const float* xv, int np, const float* shift)
+{
+    if (!ctx || !xv || !shift || np <= 0) return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    ctx->dec_n = 0;
+    const ShellIn L = shell_in_layout(np);
+    if (int r = grow(ctx, ctx->sh_in, L.total)) return r;
+    if (int r = grow(ctx, ctx->dec_raw, 24 * (size_t)np)) return r;
+    CK(cudaMemcpyAsync(ctx->dec_raw.p, xv, 24 * (size_t)np, cudaMemcpyHostToDevice, ctx->s));
+    unsigned char* b = P<unsigned char>(ctx->sh_in);
+    launch_decode_xv(P<float>(ctx->dec_raw), np, shift, reinterpret_cast<float4*>(b + L.pos),
+                     reinterpret_cast<float4*>(b + L.vel), reinterpret_cast<int*>(b + L.igrp),
+                     reinterpret_cast<float*>(b + L.rk), ctx->d_err, ctx->s);
+    if (int r = finish(ctx, "decode_xv")) return r;
+    ctx->dec_n = np;
+    return ASG_OK;
+}
+
+int asg_decode_zip(asg_ctx* ctx, const uint8_t* zip0, const int16_t* zip1, const uint8_t* zip2,
+                   const int* zip3, int n_zip3, int np_local, int nc_node_dim, int mesh_scale,
+                   float v_r2i, const float* shift)
+{
+    if (!ctx || !zip2 || !shift || (n_zip3 > 0 && !zip3) || n_zip3 < 0 || np_local < 0 ||
+        (np_local > 0 && (!zip0 || !zip1)) || nc_node_dim <= 0 || nc_node_dim > 1290 ||
+        mesh_scale <= 0)
+        return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    ctx->dec_n = 0;
+    const int nc = nc_node_dim, ncell = nc * nc * nc;
+    const size_t N = (size_t)np_local;
+    const size_t o3 = a16((size_t)ncell), o0 = o3 + a16(4 * (size_t)n_zip3), o1 = o0 + a16(3 * N);
+    if (int r = grow(ctx, ctx->dec_raw, o1 + 6 * N)) return r;
+    if (int r = grow(ctx, ctx->dec_scan, zip_scratch_bytes(ncell))) return r;
+    const ShellIn L = shell_in_layout(np_local > 0 ? np_local : 1);
+    if (int r = grow(ctx, ctx->sh_in, L.total)) return r;
+    unsigned char* raw = P<unsigned char>(ctx->dec_raw);
+    CK(cudaMemcpyAsync(raw, zip2, (size_t)ncell, cudaMemcpyHostToDevice, ctx->s));
+    if (n_zip3) CK(cudaMemcpyAsync(raw + o3, zip3, 4 * (size_t)n_zip3, cudaMemcpyHostToDevice, ctx->s));
+    if (N) {
+        CK(cudaMemcpyAsync(raw + o0, zip0, 3 * N, cudaMemcpyHostToDevice, ctx->s));
+        CK(cudaMemcpyAsync(raw + o1, zip1, 6 * N, cudaMemcpyHostToDevice, ctx->s));
+    }
+    uint32_t* start = nullptr;
+    launch_zip_counts(raw, reinterpret_cast<const int*>(raw + o3), n_zip3, ncell, ctx->dec_scan.p,
+                      &start, ctx->d_err, ctx->s);
+    CK(cudaMemcpyAsync(ctx->h_u32, start + ncell, 4, cudaMemcpyDeviceToHost, ctx->s));
+    if (int r = finish(ctx, "decode_zip counts")) return r;
+    if (ctx->h_u32[0] != (uint32_t)np_local)  // file_reader2.cpp:261-264
+        return fail(ctx, ASG_ERR_ARG, "zip cell counts sum to " + std::to_string(ctx->h_u32[0]) +
+                                          ", the header says " + std::to_string(np_local));
+    unsigned char* b = P<unsigned char>(ctx->sh_in);
+    launch_zip_particles(raw + o0, reinterpret_cast<const int16_t*>(raw + o1), start, ncell, nc,
+                         np_local, mesh_scale, v_r2i, shift, reinterpret_cast<float4*>(b + L.pos),
+                         reinterpret_cast<float4*>(b + L.vel), reinterpret_cast<int*>(b + L.igrp),
+                         reinterpret_cast<float*>(b + L.rk), ctx->s);
+    if (int r = finish(ctx, "decode_zip")) return r;
+    ctx->dec_n = np_local;
+    return ASG_OK;
+}
+
+static bool read_file(const std::string& name, std::vector<unsigned char>& out)
+{
+    FILE* fp = std::fopen(name.c_str(), "rb");
+    if (!fp) return false;
+    std::fseek(fp, 0, SEEK_END);
+    const long sz = std::ftell(fp);
+    std::fseek(fp, 0, SEEK_SET);
+    out.resize(sz > 0 ? (size_t)sz : 0);
+    const bool ok = sz >= 0 && std::fread(out.data(), 1, out.size(), fp) == out.size();
+    std::fclose(fp);
+    return ok;
+}
+
+int asg_read_pm_file_xv(asg_ctx* ctx, const char* filebase, const char* redshift, int inode,
+                        const float* shift, int* np)
+{
+    if (!ctx || !filebase || !redshift || !shift || !np) return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    const std::string i = std::to_string(inode);
+    const std::string name = std::string(filebase) + i + "/" + redshift + "xv" + i + ".dat";
+    std::vector<unsigned char> buf;
+    if (!read_file(name, buf)) return fail(ctx, ASG_ERR_IO, "cannot read " + name);
+    int n = 0;
+    if (buf.size() < 48) return fail(ctx, ASG_ERR_ARG, name + ": short header");
+    std::memcpy(&n, buf.data(), 4);  // P3m_header.np_local (file_reader2.cpp:10-14)
+    if (n <= 0 || buf.size() < 48 + 24 * (size_t)n)
+        return fail(ctx, ASG_ERR_ARG, name + ": np_local does not match the file size");
+    *np = n;
+    return asg_decode_xv(ctx, reinterpret_cast<const float*>(buf.data() + 48), n, shift);
+}
+
+int asg_read_pm_file_zip(asg_ctx* ctx, const char* filebase, const char* redshift, int inode,
+                         int nc_node_dim, int mesh_scale, const float* shift, int* np,
+                         float* boxsize)
+{
+    if (!ctx || !filebase || !redshift || !shift || !np || nc_node_dim <= 0 || nc_node_dim > 1290)
+        return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    const std::string i = std::to_string(inode);
+    std::vector<unsigned char> z[4];
+    for (int k = 0; k < 4; ++k) {
+        const std::string name = std::string(filebase) + i + "/" + redshift + "zip" +
+                                 std::to_string(k) + "_" + i + ".dat";
+        if (!read_file(name, z[k])) return fail(ctx, ASG_ERR_IO, "cannot read " + name);
+    }
+    if (z[0].size() < 64 || z[1].size() < 64) return fail(ctx, ASG_ERR_ARG, "short zip header");
+    int n = 0;
+    float v_r2i = 0.0f;
+    std::memcpy(&n, z[0].data(), 4);            // P3m_zip_header0.np_local
+    std::memcpy(&v_r2i, z[0].data() + 48, 4);   // P3m_zip_header0.v_r2i (word 12)
+    const size_t ncell = (size_t)nc_node_dim * nc_node_dim * nc_node_dim;
+    // the reference reads to the exact end of zip0 and zip1 (file_reader2.cpp:254-261)
+    if (n < 0 || z[0].size() != 64 + 3 * (size_t)n || z[1].size() != 64 + 6 * (size_t)n ||
+        z[2].size() < ncell)
+        return fail(ctx, ASG_ERR_ARG, "zip file sizes do not match np_local and nc_node_dim");
+    *np = n;
+    if (boxsize) *boxsize = (float)(mesh_scale * nc_node_dim);  // file_reader2.cpp:266
+    return asg_decode_zip(ctx, z[0].data() + 64, reinterpret_cast<const int16_t*>(z[1].data() + 64),
+                          z[2].data(), reinterpret_cast<const int*>(z[3].data()),
+                          (int)(z[3].size() / 4), n, nc_node_dim, mesh_scale, v_r2i, shift);
+}
+
+int asg_copy_decoded(asg_ctx* ctx, asg_particle* out)
+{
+    if (!ctx || !out) return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    if (ctx->dec_n <= 0) return fail(ctx, ASG_ERR_STATE, "nothing decoded");
+    CK(cudaSetDevice(ctx->device));
+    const int n = ctx->dec_n;
+    const ShellIn L = shell_in_layout(n);
+    if (int r = grow(ctx, ctx->aos, sizeof(asg_particle) * (size_t)n)) return r;
+    unsigned char* b = P<unsigned char>(ctx->sh_in);
+    launch_pack_aos(nullptr, reinterpret_cast<float4*>(b + L.pos), reinterpret_cast<float4*>(b + L.vel),
+                    reinterpret_cast<float*>(b + L.rk), nullptr, reinterpret_cast<int*>(b + L.igrp), n,
+                    ctx->aos.p, ctx->s);
+    CK(cudaMemcpyAsync(out, ctx->aos.p, sizeof(asg_particle) * (size_t)n, cudaMemcpyDeviceToHost,
+                       ctx->s));
+    return finish(ctx, "copy_decoded");
+}
+
+int asg_load_decoded_periodic(asg_ctx* ctx, float boxsize, float buffer_factor,
+                              int* np_with_buffers, int* np_local_kept)
+{
+    if (!ctx) return ASG_ERR_ARG;
+    if (ctx->dec_n <= 0) return fail(ctx, ASG_ERR_STATE, "nothing decoded");
+    if (int r = check_shell(ctx, ctx->dec_n, boxsize, buffer_factor)) return r;
+    CK(cudaSetDevice(ctx->device));
+    ctx->loaded = false;
+    return load_shell(ctx, ctx->dec_n, boxsize, buffer_factor, np_with_buffers, np_local_kept);
 }
 
 static int run_knn(asg_ctx* ctx)
@@ -909,6 +1213,93 @@ int asg_mark_halo_particles(asg_ctx* ctx, asg_particle* p, int np, const asg_hal
     if (int r = asg_load_particles(ctx, p, np, left, right)) return r;
     if (int r = asg_run_mark_halos(ctx, halos, nh, np_halo, m_halo)) return r;
     return asg_store_particles(ctx, p);
+}
+
+// ---- outputs ----------------------------------------------------------------------
+
+// FOF catalogue on device arrays indexed by j; records and count back to the host
+static int run_catalogue(asg_ctx* ctx, const float4* pos, const float4* vel, const int* igrp, int n,
+                         int w_index, int nhalo, float boxsize, asg_fof_halo* out, int* nlocal)
+{
+    const size_t rec_bytes = sizeof(asg_fof_halo) * (size_t)(nhalo > 0 ? nhalo : 1);
+    const size_t o_cnt = (rec_bytes + 15) & ~size_t(15);
+    if (int r = grow(ctx, ctx->cat, fof_catalogue_bytes(n, nhalo))) return r;
+    if (int r = grow(ctx, ctx->cat_out, o_cnt + 16)) return r;
+    unsigned char* ob = P<unsigned char>(ctx->cat_out);
+    CK(cudaMemsetAsync(ob, 0, o_cnt + 16, ctx->s));
+    launch_fof_catalogue(pos, vel, igrp, n, w_index, nhalo, boxsize, ctx->cat.p,
+                         reinterpret_cast<float*>(ob), reinterpret_cast<uint32_t*>(ob + o_cnt), ctx->s);
+    if (nhalo > 0) CK(cudaMemcpyAsync(out, ob, sizeof(asg_fof_halo) * (size_t)nhalo,
+                                      cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaMemcpyAsync(ctx->h_u32, ob + o_cnt, 4, cudaMemcpyDeviceToHost, ctx->s));
+    if (int r = finish(ctx, "fof_halos")) return r;
+    *nlocal = (int)ctx->h_u32[0];
+    return ASG_OK;
+}
+
+int asg_fof_halos(asg_ctx* ctx, const asg_particle* p, int np, int nhalo, float boxsize,
+                  asg_fof_halo* out, int* nlocal)
+{
+    if (!ctx || !p || !nlocal || (nhalo > 0 && !out) || np <= 0 || nhalo < 0 || nhalo > np)
+        return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    const size_t n = (size_t)np;
+    // staging buffers only: a loaded particle set stays valid
+    int r = grow(ctx, ctx->aos, sizeof(asg_particle) * n);
+    if (!r) r = grow(ctx, ctx->pos_in, 16 * n);
+    if (!r) r = grow(ctx, ctx->vel_in, 16 * n);
+    if (!r) r = grow(ctx, ctx->igrp_in, 4 * n);
+    if (!r) r = grow(ctx, ctx->rk_in, 4 * n);
+    if (r) return r;
+    CK(cudaMemcpyAsync(ctx->aos.p, p, sizeof(asg_particle) * n, cudaMemcpyHostToDevice, ctx->s));
+    launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
+                      P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
+    return run_catalogue(ctx, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in), P<int>(ctx->igrp_in),
+                         np, 0, nhalo, boxsize, out, nlocal);
+}
+
+int asg_run_fof_halos(asg_ctx* ctx, int nhalo, float boxsize, asg_fof_halo* out, int* nlocal)
+{
+    if (!ctx || !nlocal || (nhalo > 0 && !out) || nhalo < 0) return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    if (!ctx->loaded) return fail(ctx, ASG_ERR_STATE, "no particle set loaded");
+    if (nhalo > ctx->n) return fail(ctx, ASG_ERR_ARG, "nhalo larger than the particle count");
+    CK(cudaSetDevice(ctx->device));
+    return run_catalogue(ctx, P<float4>(ctx->pos), P<float4>(ctx->vel), P<int>(ctx->igrp), ctx->n, 1,
+                         nhalo, boxsize, out, nlocal);
+}
+
+int asg_write_fof_halos(asg_ctx* ctx, const char* filename, const asg_particle* p, int np,
+                        int nhalo, float boxsize)
+{
+    if (!filename) return fail(ctx, ASG_ERR_ARG, "null file name");
+    std::vector<asg_fof_halo> rec((size_t)(nhalo > 0 ? nhalo : 1));
+    int nl = 0;
+    if (int r = asg_fof_halos(ctx, p, np, nhalo, boxsize, rec.data(), &nl)) return r;
+    if (int r = write_fof_file(filename, reinterpret_cast<const float*>(rec.data()), nl))
+        return fail(ctx, r, std::string("cannot write ") + filename);
+    return ASG_OK;
+}
+
+int asg_write_mesh_separate(asg_ctx* ctx, const char* base, int inode, float* mesh, int nc,
+                            float boxsize)
+{
+    if (!base) return fail(ctx, ASG_ERR_ARG, "null base name");
+    if (int r = asg_normalise_mesh(ctx, mesh, nc, boxsize)) return r;
+    if (int r = write_mesh_files(base, inode, mesh, nc))
+        return fail(ctx, r, std::string("cannot write mesh files at ") + base);
+    return ASG_OK;
+}
+
+int asg_write_mesh_device(asg_ctx* ctx, int k, const char* base, int inode)
+{
+    if (!base) return fail(ctx, ASG_ERR_ARG, "null base name");
+    if (int r = asg_run_normalise(ctx, k)) return r;
+    const MeshBuf& mb = ctx->meshes[(size_t)k];
+    std::vector<float> host(mb.words);
+    if (int r = asg_copy_mesh(ctx, k, host.data())) return r;
+    if (int r = write_mesh_files(base, inode, host.data(), mb.nc))
+        return fail(ctx, r, std::string("cannot write mesh files at ") + base);
+    return ASG_OK;
 }
 
 int asg_set_timing(asg_ctx* ctx, int enable)

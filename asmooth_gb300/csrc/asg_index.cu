@@ -548,7 +548,7 @@ __global__ void k_pack_aos(const int* __restrict__ perm, const float4* __restric
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int o = perm[i];
+    const int o = perm ? perm[i] : i;  // no perm: the arrays are in output order
     const float4 p = pos[i], v = vel[i];
     float* r = reinterpret_cast<float*>(aos + o);
     r[0] = p.x; r[1] = p.y; r[2] = p.z;

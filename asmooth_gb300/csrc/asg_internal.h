@@ -150,6 +150,45 @@ void launch_count_labels(const int* igrp, int n, uint32_t* counts, cudaStream_t 
 void launch_keep_mask(uint32_t* counts, int ngrp, int threshold, cudaStream_t s);
 void launch_relabel(int* igrp, int n, const uint32_t* scan, const uint32_t* keep, cudaStream_t s);
 
+// ---- periodic buffer shell of a single-cube run (asg_shell.cu) ------------------------------
+// base[b][d]: first slot of the copies of bin b sent in direction d (-1: none)
+struct ShellPlan {
+    int base[27][27];
+};
+void launch_shell_bins(const float4* pos, int n, float lt, float rt, uint32_t* keys0, int* vals0,
+                       uint32_t* keys1, int* vals1, void* sort_tmp, uint32_t* start, uint32_t* end,
+                       const uint32_t** keys, const int** order, cudaStream_t s);
+void launch_shell_emit(const float4* pos, const float4* vel, const int* igrp, const float* rk,
+                       const uint32_t* keys, const int* order, const uint32_t* start, int n,
+                       const ShellPlan& plan, float L, float4* apos, float4* avel, int* aigrp,
+                       float* ark, cudaStream_t s);
+// keep -bf*L < x < L + bf*L; flags has n_all + 1 words and ends as the exclusive scan
+void launch_shell_filter(const float4* apos, const float4* avel, const int* aigrp, const float* ark,
+                         int n_all, float lo, float hi, uint32_t* flags, void* scan_tmp,
+                         float4* pos, float4* vel, int* igrp, float* rk, cudaStream_t s);
+
+// ---- particle file payloads (asg_decode.cu) ----------------------------------------------
+void launch_decode_xv(const float* xv, int n, const float* shift, float4* pos, float4* vel,
+                      int* igrp, float* rk, int* err, cudaStream_t s);
+size_t zip_scratch_bytes(int ncell);
+// *start: first particle of every cell, ncell + 1 entries (the last = total)
+void launch_zip_counts(const uint8_t* c8, const int* c32, int n32, int ncell, void* scratch,
+                       uint32_t** start, int* err, cudaStream_t s);
+void launch_zip_particles(const uint8_t* off, const int16_t* vq, const uint32_t* start, int ncell,
+                          int nc, int n, int mesh_scale, float v_r2i, const float* shift,
+                          float4* pos, float4* vel, int* igrp, float* rk, cudaStream_t s);
+
+// ---- FOF halo catalogue and file formats (asg_output.cu) ----------------------------------
+// records {x[3], v[3], int nfof} of labels 1..nhalo with centre inside (0, boxsize)^3, label
+// order, into out (device, 7*nhalo words) and *nlocal (device); pos/vel/igrp indexed by j,
+// the caller's array index is pos[j].w when w_index else j
+size_t fof_catalogue_bytes(int n, int nhalo);
+void launch_fof_catalogue(const float4* pos, const float4* vel, const int* igrp, int n, int w_index,
+                          int nhalo, float boxsize, void* scratch, float* out, uint32_t* nlocal,
+                          cudaStream_t s);
+int write_mesh_files(const char* base, int inode, const float* mesh, int nc);
+int write_fof_file(const char* filename, const float* rec, int nlocal);
+
 // ---- output (asg_index.cu) ------------------------------------------------------------
 // write reference Particle records in input order from the sorted fields
 void launch_pack_aos(const int* perm, const float4* pos, const float4* vel, const float* rk,

@@ -212,6 +212,56 @@ def write_xv(path: str, x: np.ndarray, v: np.ndarray) -> None:
         f.write(np.concatenate([x, v], axis=1).astype("<f4").tobytes())
 
 
+def zip_paths(filebase: str, redshift: str, inode: int) -> list[str]:
+    """<filebase><inode>/<redshift>zip{0,1,2,3}_<inode>.dat (file_reader2.cpp:155-165)."""
+    return [f"{filebase}{inode}/{redshift}zip{k}_{inode}.dat" for k in range(4)]
+
+
+def xv_path(filebase: str, redshift: str, inode: int) -> str:
+    """<filebase><inode>/<redshift>xv<inode>.dat (file_reader2.cpp:33)."""
+    return f"{filebase}{inode}/{redshift}xv{inode}.dat"
+
+
+def write_zip(filebase: str, redshift: str, inode: int, x: np.ndarray, v: np.ndarray,
+              nc_node_dim: int, mesh_scale: int, v_r2i: float,
+              shift=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """cubep3m zipped particles as read by read_pm_file_zip (file_reader2.cpp:90-272),
+    little endian: zip0 = 64-byte header (int np_local, float ... v_r2i at word
+    12) + 3 uint8 offsets per particle, zip1 = 64-byte header + 3 int16
+    velocities, zip2 = one uint8 count per fine cell (x fastest, 255 = the
+    count is the next int32 of zip3), zip3 = those int32 counts.  Positions are
+    quantised to 1/256 of a cell of side mesh_scale, velocities to 1/v_r2i.
+    Returns the input index of each stored particle (storage order = cell order)."""
+    import os
+
+    x = np.asarray(x, np.float64) + np.asarray(shift, np.float64)
+    n = x.shape[0]
+    g = nc_node_dim
+    rel = x / mesh_scale
+    c = np.clip(np.floor(rel).astype(np.int64), 0, g - 1)
+    off = np.clip(np.floor((rel - c) * 256.0), 0, 255).astype(np.uint8)
+    cell = (c[:, 2] * g + c[:, 1]) * g + c[:, 0]
+    order = np.argsort(cell, kind="stable")
+    counts = np.bincount(cell, minlength=g ** 3)
+    vi = np.clip(np.rint(np.asarray(v, np.float64) * v_r2i), -32768, 32767).astype("<i2")
+    paths = zip_paths(filebase, redshift, inode)
+    os.makedirs(os.path.dirname(paths[0]) or ".", exist_ok=True)
+    head0 = np.zeros(16, "<f4")
+    head0.view("<i4")[0] = n
+    head0[12] = v_r2i
+    with open(paths[0], "wb") as f:
+        f.write(head0.tobytes())
+        f.write(off[order].tobytes())
+    with open(paths[1], "wb") as f:
+        f.write(np.zeros(16, "<f4").tobytes())
+        f.write(vi[order].tobytes())
+    with open(paths[2], "wb") as f:
+        f.write(np.minimum(counts, 255).astype(np.uint8).tobytes())
+    with open(paths[3], "wb") as f:
+        f.write(counts[counts >= 255].astype("<i4").tobytes())
+    return order
+
+
 def read_xv(path: str) -> tuple[np.ndarray, np.ndarray]:
     with open(path, "rb") as f:
         n = struct.unpack("<i", f.read(4))[0]

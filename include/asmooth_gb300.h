@@ -52,7 +52,8 @@ enum {
     ASG_ERR_RANGE = -9,       /* periodic deposit: kernel support wider than the mesh */
     ASG_ERR_STATE = -10,      /* call needs a previous step (e.g. deposit before search) */
     ASG_ERR_UNIONFIND = -11,  /* FOF union-find retry limit reached */
-    ASG_ERR_NOALLOC_LIMIT = -12 /* input larger than the allocation-free entry point's fixed scratch */
+    ASG_ERR_NOALLOC_LIMIT = -12, /* input larger than the allocation-free entry point's fixed scratch */
+    ASG_ERR_IO = -13            /* an output file could not be opened or written */
 };
 
 /* ---- context ------------------------------------------------------------- */
@@ -122,6 +123,40 @@ int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, f
                const asg_halo* halos, int nh, const int* ncs, int n_nc, int sign,
                float* const* meshes, double* totals, long* np_halo, double* m_halo);
 
+/* ---- outputs ------------------------------------------------------------------ */
+
+/* write_mesh_separate (coarse_mesh.cpp:147-208, called at
+ * clumping_tree_main.cpp:446-447 and :531-532): normalises the host mesh in
+ * place (as asg_normalise_mesh) and writes <base>n<inode>.dat,
+ * <base>h<inode>.dat, <base>c<inode>.dat (int nc, nc^3 floats each) and
+ * <base>vel<inode>.dat (int nc, 3*nc^3 floats), byte for byte the reference's
+ * files.  The directories must exist.  ASG_ERR_IO when a file fails. */
+int asg_write_mesh_separate(asg_ctx* ctx, const char* base, int inode, float* mesh, int nc,
+                            float boxsize);
+/* The same for device mesh k of the last asg_run_deposit (normalised in place). */
+int asg_write_mesh_device(asg_ctx* ctx, int k, const char* base, int inode);
+/* write_mesh (coarse_mesh.cpp:128-143): int nc, int 6, float boxsize, then the
+ * 6*nc^3 floats of the mesh as they are.  Host only. */
+int asg_write_mesh(const char* filename, const float* mesh, int nc, float boxsize);
+
+/* struct FofHalo (fof.cpp:22-25), 28 bytes */
+typedef struct asg_fof_halo {
+    float x[3], v[3];
+    int nfof;
+} asg_fof_halo;
+
+/* The catalogue of write_fof_halos (fof.cpp:169-219) for labels 1..nhalo (the
+ * output of asg_remove_small_groups): per halo the float sums of x and v over
+ * its members in array order divided by the member count; halos whose centre
+ * is strictly inside (0, boxsize)^3 go to out[0..*nlocal-1] in label order
+ * (out holds nhalo records).  Same bits as the reference on the same array,
+ * except that v[2] starts from 0 (the reference never clears it, fof.cpp:179). */
+int asg_fof_halos(asg_ctx* ctx, const asg_particle* p, int np, int nhalo, float boxsize,
+                  asg_fof_halo* out, int* nlocal);
+/* write_fof_halos' file: int nlocal, int 28, the records, int nlocal. */
+int asg_write_fof_halos(asg_ctx* ctx, const char* filename, const asg_particle* p, int np,
+                        int nhalo, float boxsize);
+
 /* ---- staged device-resident interface --------------------------------------- */
 
 /* Load a particle set and build its index (H2D + sort + tree).  Subsequent
@@ -132,11 +167,63 @@ int asg_load_particles(asg_ctx* ctx, const asg_particle* p, int np, float left, 
 int asg_load_particles_device(asg_ctx* ctx, const float* d_x, const float* d_v,
                               const float* d_dens, const int* d_igrp, int np, float left,
                               float right);
+/* Single-cube periodic run: the np_local particles of the whole box [0, L)^3
+ * plus the buffer shell built on the device, replacing the one-rank
+ * exchange_buffer (exchange_buffer.cpp:13-168, every direction a
+ * self-exchange with x -= (d-1)*L) and remove_extra_particles
+ * (clumping_tree_main.cpp:550-576, keep -bf*L < x < L + bf*L), then the index
+ * build as asg_load_particles with left = -bf*L, right = L + bf*L.  The same
+ * particles and float positions as the reference; order: the np_local
+ * particles as given, then the copies grouped by (source bin, direction) in
+ * the reference's loop order, each group in input order (the reference orders
+ * a bin by an in-place swap sort).  *np_with_buffers receives the set size
+ * (read it back with asg_store_particles into that many records),
+ * *np_local_kept the interior particles kept. */
+int asg_load_periodic_cube(asg_ctx* ctx, const asg_particle* p, int np_local, float boxsize,
+                           float buffer_factor, int* np_with_buffers, int* np_local_kept);
+int asg_load_periodic_cube_device(asg_ctx* ctx, const float* d_x, const float* d_v, int np_local,
+                                  float boxsize, float buffer_factor, int* np_with_buffers,
+                                  int* np_local_kept);
+
+/* ---- particle files decoded on the device ------------------------------------
+ * The conversion of read_pm_file_xv (file_reader2.cpp:24-86: x - shift, v,
+ * rk = dens = igrp = 0) and the count-prefix expansion of read_pm_file_zip
+ * (file_reader2.cpp:90-272: x = mesh_scale*((off + 0.5f)/256.0f + i - 1.0f)
+ * - shift in that float order, v = vel / v_r2i; little-endian files) run on
+ * the device; the decoded particles stay there for asg_load_decoded_periodic
+ * and can be read back with asg_copy_decoded. */
+/* xv: np records of 6 floats (x, y, z, vx, vy, vz), the payload after the 48-byte header. */
+int asg_decode_xv(asg_ctx* ctx, const float* xv, int np, const float* shift);
+/* zip: zip0 payload (3*np_local offsets), zip1 payload (3*np_local int16), zip2
+ * (nc_node_dim^3 counts), zip3 (n_zip3 int32 counts of the cells marked 255).
+ * ASG_ERR_ARG when the counts do not sum to np_local (the reference's
+ * ErrorParticleReader) or a 255-cell has no zip3 entry. */
+int asg_decode_zip(asg_ctx* ctx, const uint8_t* zip0, const int16_t* zip1, const uint8_t* zip2,
+                   const int* zip3, int n_zip3, int np_local, int nc_node_dim, int mesh_scale,
+                   float v_r2i, const float* shift);
+/* read_pm_file_xv / read_pm_file_zip (file_reader2.h): read
+ * <filebase><inode>/<redshift>xv<inode>.dat or <redshift>zip{0..3}_<inode>.dat
+ * on the host and decode on the device; *np = np_local, *boxsize = mesh_scale *
+ * nc_node_dim (zip).  ASG_ERR_IO when a file cannot be read, ASG_ERR_ARG when
+ * sizes disagree (the reference asserts). */
+int asg_read_pm_file_xv(asg_ctx* ctx, const char* filebase, const char* redshift, int inode,
+                        const float* shift, int* np);
+int asg_read_pm_file_zip(asg_ctx* ctx, const char* filebase, const char* redshift, int inode,
+                         int nc_node_dim, int mesh_scale, const float* shift, int* np,
+                         float* boxsize);
+/* The decoded particles as Particle records (np of them, in file order). */
+int asg_copy_decoded(asg_ctx* ctx, asg_particle* out);
+/* asg_load_periodic_cube on the decoded particles, without a host round trip. */
+int asg_load_decoded_periodic(asg_ctx* ctx, float boxsize, float buffer_factor,
+                              int* np_with_buffers, int* np_local_kept);
+
 int asg_run_neighbor_search(asg_ctx* ctx);
 int asg_run_mark_halos(asg_ctx* ctx, const asg_halo* halos, int nh, long* np_halo,
                        double* m_halo);
 int asg_run_fof(asg_ctx* ctx, float ll, int* ngroup);
 int asg_run_remove_small_groups(asg_ctx* ctx, int ngrp, int* nhalo);
+/* Catalogue of the loaded set's labels (as asg_fof_halos), array order = load order. */
+int asg_run_fof_halos(asg_ctx* ctx, int nhalo, float boxsize, asg_fof_halo* out, int* nlocal);
 /* Deposit for every nc into library-owned device meshes (read them with
  * asg_mesh_device or asg_copy_mesh); totals (host, 2 per mesh) optional. */
 int asg_run_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,

@@ -776,6 +776,78 @@ int orc_remove_small_groups(int* igrp, int n, int ngrp, int* nhalo)
     return 0;
 }
 
+/* Zipped particle decode (read_pm_file_zip, file_reader2.cpp:187-252): fine
+ * cells in (k, j, i) order, x fastest, each with counts8[cell] particles or,
+ * for 255, the next value of counts32; particle p at
+ *   x = mesh_scale*((off[3p] + 0.5f)/256.0f + i - 1.0f) - shift[0]   (i 1-based)
+ *   v = vel[3p] / v_r2i
+ * Returns 0 when exactly np_local particles are decoded, -1 otherwise. */
+int orc_decode_zip(const unsigned char* off, const short* vel, const unsigned char* counts8,
+                   const int* counts32, int n32, int np_local, int nc, int mesh_scale, float v_r2i,
+                   const float* shift, float* x, float* v)
+{
+    int np = 0, j3 = 0;
+    size_t cell = 0;
+    for (int k = 1; k <= nc; ++k)
+        for (int j = 1; j <= nc; ++j)
+            for (int i = 1; i <= nc; ++i, ++cell) {
+                int rr = counts8[cell];
+                if (rr == 255) {
+                    if (j3 >= n32) return -1;
+                    rr = counts32[j3++];
+                }
+                for (int l = 1; l <= rr; ++l, ++np) {
+                    if (np >= np_local) return -1;
+                    const int c[3] = {i, j, k};
+                    for (int d = 0; d < 3; ++d) {
+                        x[3 * (size_t)np + d] =
+                            mesh_scale * ((off[3 * (size_t)np + d] + 0.5f) / 256.0f + c[d] - 1.0f) -
+                            shift[d];
+                        v[3 * (size_t)np + d] = vel[3 * (size_t)np + d] / v_r2i;
+                    }
+                }
+            }
+    return np == np_local ? 0 : -1;
+}
+
+/* FOF halo catalogue (write_fof_halos, fof.cpp:169-219): per label 1..nhalo
+ * the float sums of x and v in array order (fof.cpp:183-193), divided by the
+ * member count (:199-202); halos whose centre is strictly inside (0, boxsize)^3
+ * are kept in label order (:203-207).  out holds nhalo records of 7 words
+ * {x[3], v[3], (int) nfof}.  The reference never clears v[2] (:179 clears x[2]
+ * twice); here it starts at 0, which is what the reference gives on a zeroed
+ * buffer. */
+int orc_fof_halos(const float* x, const float* v, const int* igrp, int n, int nhalo,
+                  float boxsize, float* out, int* nlocal)
+{
+    if (!x || !v || !igrp || !out || !nlocal || n < 0 || nhalo < 0) return -1;
+    float* h = (float*)calloc((size_t)nhalo + 1, 7 * sizeof(float));
+    int* nf = (int*)calloc((size_t)nhalo + 1, sizeof(int));
+    if (!h || !nf) { free(h); free(nf); return -2; }
+    for (int j = 0; j < n; ++j) {
+        const int i = igrp[j] - 1;
+        if (i < 0 || i >= nhalo) continue;
+        nf[i]++;
+        for (int k = 0; k < 3; ++k) {
+            h[7 * i + k] += x[3 * j + k];
+            h[7 * i + 3 + k] += v[3 * j + k];
+        }
+    }
+    int nl = 0;
+    for (int j = 0; j < nhalo; ++j) {
+        float r[7];
+        for (int k = 0; k < 6; ++k) r[k] = h[7 * j + k] / (float)nf[j];
+        memcpy(&r[6], &nf[j], 4);
+        if (0.0f < r[0] && r[0] < boxsize && 0.0f < r[1] && r[1] < boxsize && 0.0f < r[2] &&
+            r[2] < boxsize)
+            memcpy(out + 7 * (size_t)nl++, r, sizeof r);
+    }
+    *nlocal = nl;
+    free(h);
+    free(nf);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------- */
 /* SO-halo marking (nbr_search.cpp:140-165, clumping_tree_main.cpp:474-485)    */
 /* ------------------------------------------------------------------------- */

@@ -86,6 +86,16 @@ int orc_group_fof(const float* x, int n, float left, float right, float ll, int 
  * in label order, all others -> 0. */
 int orc_remove_small_groups(int* igrp, int n, int ngrp, int* nhalo);
 
+/* Zipped particle decode of read_pm_file_zip (file_reader2.cpp:187-252). */
+int orc_decode_zip(const unsigned char* off, const short* vel, const unsigned char* counts8,
+                   const int* counts32, int n32, int np_local, int nc, int mesh_scale, float v_r2i,
+                   const float* shift, float* x, float* v);
+
+/* FOF halo catalogue of write_fof_halos (fof.cpp:169-219): out gets up to
+ * nhalo records {x[3], v[3], int nfof} (7 words), *nlocal of them kept. */
+int orc_fof_halos(const float* x, const float* v, const int* igrp, int n, int nhalo,
+                  float boxsize, float* out, int* nlocal);
+
 /* Faithful SO-halo marking: the loop at clumping_tree_main.cpp:474-485 around
  * mark_halo_particles (nbr_search.cpp:140-165).  halos: 5 floats per halo
  * (x, y, z, r, mass) = struct Halo (basic_types.h:17-20).  Halos whose centre is

@@ -17,7 +17,7 @@ OUT="$HERE/_ref"
 mkdir -p "$OUT"
 SRCS=""
 for f in nbr_search.cpp kdtree_balanced.cpp coarse_mesh.cpp fof.cpp basic_types.cpp \
-         open.cpp global_mesh.cpp mpi_interface.cpp; do
+         open.cpp global_mesh.cpp mpi_interface.cpp exchange_buffer.cpp file_reader2.cpp; do
     SRCS="$SRCS $REF/$f"
 done
 # -iquote: the reference's endian.h must not shadow the system <endian.h>

@@ -15,6 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORC_SO = os.path.join(HERE, "liborc.so")
 REF_DIR = os.path.join(HERE, "_ref")
 K = 33
+# struct FofHalo (fof.cpp:22-25): 28 bytes
+FOF_HALO_DTYPE = np.dtype([("x", "<f4", (3,)), ("v", "<f4", (3,)), ("nfof", "<i4")])
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -50,7 +52,8 @@ class Oracle:
         L = self.lib
         for name in ("orc_neighbor_search", "orc_knn_exact", "orc_dens_from_lists",
                      "orc_assign_on_mesh", "orc_assign_on_density_mesh", "orc_normalise_mesh",
-                     "orc_group_fof", "orc_remove_small_groups", "orc_mark_halo_particles"):
+                     "orc_group_fof", "orc_remove_small_groups", "orc_mark_halo_particles",
+                     "orc_fof_halos", "orc_decode_zip"):
             getattr(L, name).restype = C.c_int
         L.orc_mesh_total.restype = C.c_double
 
@@ -151,6 +154,39 @@ class Oracle:
             raise RuntimeError("orc_remove_small_groups failed")
         return g, nh.value
 
+    def decode_zip(self, filebase, redshift, inode, nc_node_dim, mesh_scale, shift=(0, 0, 0)):
+        """Read the four zip files and decode them as read_pm_file_zip: (x, v, boxsize)."""
+        paths = [f"{filebase}{inode}/{redshift}zip{k}_{inode}.dat" for k in range(4)]
+        b0, b1 = open(paths[0], "rb").read(), open(paths[1], "rb").read()
+        n = int(np.frombuffer(b0[:4], "<i4")[0])
+        v_r2i = float(np.frombuffer(b0[48:52], "<f4")[0])
+        off = np.frombuffer(b0[64:], np.uint8).copy()
+        vel = np.frombuffer(b1[64:], "<i2").copy()
+        c8 = np.frombuffer(open(paths[2], "rb").read(), np.uint8).copy()
+        c32 = np.frombuffer(open(paths[3], "rb").read(), "<i4").copy()
+        sh = np.asarray(shift, np.float32)
+        x = np.zeros((n, 3), np.float32)
+        v = np.zeros((n, 3), np.float32)
+        rc = self.lib.orc_decode_zip(_p(off), _p(vel), _p(c8), _p(c32), C.c_int(c32.size), C.c_int(n),
+                                     C.c_int(nc_node_dim), C.c_int(mesh_scale), C.c_float(v_r2i),
+                                     _p(sh), _p(x), _p(v))
+        if rc:
+            raise RuntimeError("orc_decode_zip failed")
+        return x, v, np.float32(mesh_scale * nc_node_dim)
+
+    def fof_halos(self, x, v, igrp, nhalo, boxsize):
+        """write_fof_halos' catalogue: records of FOF_HALO_DTYPE, centre inside the cube."""
+        x = np.ascontiguousarray(x, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        g = np.ascontiguousarray(igrp, np.int32)
+        out = np.zeros(max(nhalo, 1), FOF_HALO_DTYPE)
+        nl = C.c_int(0)
+        rc = self.lib.orc_fof_halos(_p(x), _p(v), _p(g), C.c_int(g.size), C.c_int(nhalo),
+                                    C.c_float(boxsize), _p(out), C.byref(nl))
+        if rc:
+            raise RuntimeError("orc_fof_halos failed")
+        return out[:nl.value].copy()
+
     def mark_halo_particles(self, x, left, right, halos, igrp=None, exact=False):
         x = np.ascontiguousarray(x, np.float32)
         n = x.shape[0]
@@ -227,6 +263,54 @@ class Reference:
         self.lib.ref_write_mesh_separate(C.c_char_p(base.encode()), C.c_int(inode), _p(m),
                                          C.c_int(nc), C.c_float(boxsize))
         return m
+
+    def read_pm_file_zip(self, filebase, redshift, inode, nc_node_dim, mesh_scale, cap,
+                         shift=(0, 0, 0)):
+        x, v = np.zeros((cap, 3), np.float32), np.zeros((cap, 3), np.float32)
+        n, L = C.c_int(0), C.c_float(0)
+        sh = np.asarray(shift, np.float32)
+        rc = self.lib.ref_read_pm_file_zip(filebase.encode(), redshift.encode(), C.c_int(inode),
+                                           C.c_int(nc_node_dim), C.c_int(mesh_scale), _p(sh),
+                                           C.c_int(cap), _p(x), _p(v), C.byref(n), C.byref(L))
+        if rc:
+            raise RuntimeError("ref_read_pm_file_zip failed")
+        return x[:n.value].copy(), v[:n.value].copy(), np.float32(L.value)
+
+    def read_pm_file_xv(self, filebase, redshift, inode, cap, shift=(0, 0, 0)):
+        x, v = np.zeros((cap, 3), np.float32), np.zeros((cap, 3), np.float32)
+        n = C.c_int(0)
+        sh = np.asarray(shift, np.float32)
+        rc = self.lib.ref_read_pm_file_xv(filebase.encode(), redshift.encode(), C.c_int(inode),
+                                          _p(sh), C.c_int(cap), _p(x), _p(v), C.byref(n))
+        if rc:
+            raise RuntimeError("ref_read_pm_file_xv failed")
+        return x[:n.value].copy(), v[:n.value].copy()
+
+    def exchange_buffer(self, x, v, boxsize, buffer_factor):
+        """One-rank exchange_buffer + remove_extra_particles: (x, v, np_local)."""
+        x = np.ascontiguousarray(x, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        cap = 8 * len(x) + 1024
+        ox, ov = np.zeros((cap, 3), np.float32), np.zeros((cap, 3), np.float32)
+        nw, nl = C.c_int(0), C.c_int(0)
+        rc = self.lib.ref_exchange_buffer(_p(x), _p(v), C.c_int(len(x)), C.c_float(boxsize),
+                                          C.c_float(buffer_factor), _p(ox), _p(ov), C.c_int(cap),
+                                          C.byref(nw), C.byref(nl))
+        if rc:
+            raise RuntimeError("ref_exchange_buffer failed")
+        return ox[:nw.value].copy(), ov[:nw.value].copy(), nl.value
+
+    def write_mesh(self, filename, mesh, nc, boxsize):
+        m = np.array(mesh, np.float32)
+        self.lib.ref_write_mesh(C.c_char_p(filename.encode()), _p(m), C.c_int(nc),
+                                C.c_float(boxsize))
+
+    def write_fof_halos(self, filename, x, v, igrp, nhalo, boxsize):
+        self.lib.ref_write_fof_halos(C.c_char_p(filename.encode()),
+                                     _p(np.ascontiguousarray(x, np.float32)),
+                                     _p(np.ascontiguousarray(v, np.float32)),
+                                     _p(np.ascontiguousarray(igrp, np.int32)),
+                                     C.c_int(len(igrp)), C.c_int(nhalo), C.c_float(boxsize))
 
     def group_fof(self, x, left, right, ll):
         x = np.ascontiguousarray(x, np.float32)

@@ -15,6 +15,8 @@
 
 #include "basic_types.h"
 #include "coarse_mesh.h"
+#include "exchange_buffer.h"
+#include "file_reader2.h"
 #include "fof.h"
 #include "k_neighbors.h"
 #include "kdtree_balanced.h"
@@ -158,6 +160,119 @@ double ref_mesh_total(const float* mesh, int nc) { return mesh_total(mesh, nc); 
 int ref_write_mesh_separate(const char* base, int inode, float* mesh, int nc, float boxsize)
 {
     write_mesh_separate(base, inode, mesh, nc, boxsize);
+    return 0;
+}
+
+/* The single-rank periodic shell: exchange_buffer (exchange_buffer.cpp:13-168)
+ * on one rank of a 1x1x1 periodic grid, every direction a self-exchange, then
+ * the filter of remove_extra_particles (clumping_tree_main.cpp:550-576, a
+ * static function of the driver, replayed here).  Out arrays hold cap
+ * particles; returns -1 when they are too small. */
+int ref_exchange_buffer(const float* x, const float* v, int n, float boxsize, float buffer_factor,
+                        float* out_x, float* out_v, int cap, int* n_with, int* n_local)
+{
+    const int alloc = 8 * n + 1024;  /* the shell is at most 26/27 x 7 copies */
+    Particles* ps = make_particles(alloc);
+    ps->np_local = n;
+    ps->np_with_buffers = n;
+    ps->np_allocated = alloc;
+    ps->boxsize = boxsize;
+    Particle* p = ps->particle;
+    for (int i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            p[i].x[d] = x[3 * i + d];
+            p[i].v[d] = v[3 * i + d];
+        }
+    MpiInterface mpi;
+    exchange_buffer(&mpi, ps, buffer_factor);
+    /* remove_extra_particles */
+    const float dx = buffer_factor * ps->boxsize;
+    const float left = -dx, right = ps->boxsize + dx;
+    int kept = 0, local = n;
+    for (int i = 0; i < ps->np_with_buffers; ++i) {
+        const Particle& q = p[i];
+        if (left < q.x[0] && q.x[0] < right && left < q.x[1] && q.x[1] < right && left < q.x[2] &&
+            q.x[2] < right) {
+            if (kept >= cap) { free_particles(ps); return -1; }
+            for (int d = 0; d < 3; ++d) {
+                out_x[3 * kept + d] = q.x[d];
+                out_v[3 * kept + d] = q.v[d];
+            }
+            ++kept;
+        } else if (i < n) {
+            --local;
+        }
+    }
+    *n_with = kept;
+    *n_local = local;
+    free_particles(ps);
+    return 0;
+}
+
+/* read_pm_file_xv / read_pm_file_zip (file_reader2.cpp:24-86, :90-272): the
+ * particles of <filebase><inode>/<redshift>{xv,zip0..3_}<inode>.dat, up to cap */
+static int copy_out(Particles* ps, float* x, float* v, int cap, int* np)
+{
+    const int n = (int)ps->np_local;
+    if (n > cap) return -1;
+    for (int i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            x[3 * i + d] = ps->particle[i].x[d];
+            v[3 * i + d] = ps->particle[i].v[d];
+        }
+    *np = n;
+    return 0;
+}
+
+int ref_read_pm_file_xv(const char* filebase, const char* redshift, int inode, const float* shift,
+                        int cap, float* x, float* v, int* np)
+{
+    Particles* ps = make_particles(cap + 8);
+    read_pm_file_xv(filebase, redshift, inode, 0.0f, shift, ps);
+    const int r = copy_out(ps, x, v, cap, np);
+    free_particles(ps);
+    return r;
+}
+
+int ref_read_pm_file_zip(const char* filebase, const char* redshift, int inode, int nc_node_dim,
+                         int mesh_scale, const float* shift, int cap, float* x, float* v, int* np,
+                         float* boxsize)
+{
+    Particles* ps = make_particles(cap + 8);
+    read_pm_file_zip(filebase, redshift, inode, 0.0f, nc_node_dim, mesh_scale, shift, ps);
+    *boxsize = ps->boxsize;
+    const int r = copy_out(ps, x, v, cap, np);
+    free_particles(ps);
+    return r;
+}
+
+/* write_mesh (coarse_mesh.cpp:128-143): int nc, int dof, float boxsize, mesh */
+int ref_write_mesh(const char* filename, float* mesh, int nc, float boxsize)
+{
+    write_mesh(const_cast<char*>(filename), mesh, nc, boxsize);
+    return 0;
+}
+
+/* write_fof_halos (fof.cpp:169-219) on particles in the caller's order, with a
+ * zeroed work buffer (the function never clears v[2] itself) */
+int ref_write_fof_halos(const char* filename, const float* x, const float* v, const int* igrp,
+                        int n, int nhalo, float boxsize)
+{
+    Particles* ps = make_particles(n);
+    ps->boxsize = boxsize;
+    Particle* p = ps->particle;
+    for (int i = 0; i < n; ++i) {
+        for (int d = 0; d < 3; ++d) {
+            p[i].x[d] = x[3 * i + d];
+            p[i].v[d] = v[3 * i + d];
+        }
+        p[i].igrp = igrp[i];
+    }
+    const size_t words = std::max((size_t)n, 7 * ((size_t)nhalo + 2));
+    float* buf = (float*)std::calloc(words, sizeof(float));
+    write_fof_halos(filename, ps, buf, nhalo);
+    std::free(buf);
+    free_particles(ps);
     return 0;
 }
 

@@ -1,0 +1,33 @@
+"""The periodic buffer shell of a single-cube run: the host restatement
+(synthetic.add_periodic_shell, the definition the device builder follows)
+against the reference's own one-rank exchange_buffer + remove_extra_particles."""
+import numpy as np
+import pytest
+
+import pyoracle as po
+
+from asmooth_gb300 import synthetic as syn
+
+needs_ref = pytest.mark.skipif(not po.Reference.available(), reason="reference harness not built")
+
+
+def _rows(x, v):
+    a = np.concatenate([x, v], axis=1)
+    return a[np.lexsort(a.T[::-1])]
+
+
+@needs_ref
+@pytest.mark.parametrize("L,b,n", [(64.0, 8.0, 20000), (128.0, 8.0, 30000), (40.0, 6.5, 5000)])
+def test_shell_matches_reference_exchange(L, b, n):
+    rng = np.random.default_rng(int(L))
+    x = rng.uniform(0, L, (n, 3)).astype(np.float32)
+    x[:50] = rng.choice([0.0, np.float32(b), np.float32(L - b), np.nextafter(np.float32(L), 0)],
+                        size=(50, 3))  # exactly on the bin thresholds and the faces
+    v = rng.normal(size=(n, 3)).astype(np.float32)
+    bf = np.float32(np.float32(b) / np.float32(L))
+    rx, rv, rn = po.Reference().exchange_buffer(x, v, L, bf)
+    cube = syn.add_periodic_shell(x, v, L, b)
+    assert cube.n == len(rx) and cube.n_local == rn == n
+    # interior particles first, in input order; the same shell particles, bit for bit
+    assert np.array_equal(cube.x[:n], rx[:n]) and np.array_equal(cube.v[:n], rv[:n])
+    assert np.array_equal(_rows(cube.x, cube.v), _rows(rx, rv))
