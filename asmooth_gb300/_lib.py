@@ -43,6 +43,13 @@ SIGNATURES = {
     "asg_read_pm_file_zip": (_i, [_vp, C.c_char_p, C.c_char_p, _i, _i, _i, _vp, _ip, _fp]),
     "asg_copy_decoded": (_i, [_vp, _vp]),
     "asg_load_decoded_periodic": (_i, [_vp, _f, _f, _ip, _ip]),
+    "asg_batch_create": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, C.POINTER(_vp)]),
+    "asg_batch_destroy": (None, [_vp]),
+    "asg_batch_set_item": (_i, [_vp, _i, _vp, _vp, _i]),
+    "asg_batch_tune": (_i, [_vp, _ip, _ip]),
+    "asg_batch_run": (_i, [_vp]),
+    "asg_batch_stats": (_i, [_vp, _dp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "asg_batch_get": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "asg_load_particles": (_i, [_vp, _vp, _i, _f, _f]),
     "asg_load_particles_device": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _f, _f]),
     "asg_load_particles_quantised": (_i, [_vp, _vp, _vp, _vp, _i, _f, _f, _f, _i]),

@@ -441,6 +441,67 @@ class Context:
         return t33, idx33
 
 
+class Batch:
+    """The batched form: many cubes (``synthetic.Cube``-like objects with x, v,
+    n, n_local, left, right, boxsize) through the whole path in one CUDA graph,
+    on one context (used exclusively until ``close``)."""
+
+    def __init__(self, ctx: Context, cubes, ncs, sign: int = -1):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.ncs = [int(nc) for nc in ncs]
+        self.n = [int(c.n) for c in cubes]
+        arr = lambda vals, dt: np.asarray(vals, dt)  # noqa: E731
+        npa, nla = arr(self.n, np.int32), arr([c.n_local for c in cubes], np.int32)
+        lf, rt = arr([c.left for c in cubes], np.float32), arr([c.right for c in cubes], np.float32)
+        bx, nca = arr([c.boxsize for c in cubes], np.float32), arr(self.ncs, np.int32)
+        h = C.c_void_p()
+        ctx._ok(self.lib.asg_batch_create(ctx.h, len(cubes), _ptr(npa), _ptr(nla), _ptr(lf), _ptr(rt),
+                                          _ptr(bx), _ptr(nca), len(self.ncs), int(sign), C.byref(h)))
+        self.h = h
+        for i, c in enumerate(cubes):
+            self.set_item(i, c.x, c.v)
+
+    def set_item(self, i: int, x: np.ndarray, v: np.ndarray | None = None):
+        x = np.ascontiguousarray(x, np.float32)
+        v = None if v is None else np.ascontiguousarray(v, np.float32)
+        if x.shape != (self.n[i], 3):
+            raise ValueError("item size is fixed at creation")
+        self.ctx._ok(self.lib.asg_batch_set_item(self.h, int(i), _ptr(x), _ptr(v), 0))
+
+    def tune(self):
+        leaf, seg = C.c_int(0), C.c_int(0)
+        self.ctx._ok(self.lib.asg_batch_tune(self.h, C.byref(leaf), C.byref(seg)))
+        return leaf.value, seg.value
+
+    def run(self):
+        self.ctx._ok(self.lib.asg_batch_run(self.h))
+
+    def stats(self) -> dict:
+        ms, k, nl = C.c_double(0.0), C.c_longlong(0), C.c_longlong(0)
+        self.ctx._ok(self.lib.asg_batch_stats(self.h, C.byref(ms), C.byref(k), C.byref(nl)))
+        return {"graph_ms": ms.value, "kernels": k.value, "particles_local": nl.value}
+
+    def get(self, i: int):
+        n = self.n[i]
+        rk, dens = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        meshes = [np.zeros(6 * nc ** 3, np.float32) for nc in self.ncs]
+        arrp = (C.c_void_p * len(meshes))(*[m.ctypes.data for m in meshes])
+        tot = np.zeros(2 * len(self.ncs), np.float64)
+        self.ctx._ok(self.lib.asg_batch_get(self.h, int(i), _ptr(rk), _ptr(dens), arrp, _ptr(tot)))
+        return rk, dens, meshes, tot.reshape(-1, 2)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.asg_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 _DEFAULT: Context | None = None
 
 

@@ -49,14 +49,16 @@ struct asg_ctx {
     // loaded particle set
     int n = 0;
     float left = 0.f, right = 0.f;
-    bool loaded = false, knn_done = false, ebox_valid = false, idx33_all = false;
+    bool loaded = false, knn_done = false, rk_checked = false, idx33_all = false;
     int leaf = 32;  // tree bucket size scanned whole by the traversals (fastest on GB300)
+    int dep_seg = 4096;  // pairs per deposit work item
     int* perm = nullptr;       // sorted position -> input index
     uint64_t* keys = nullptr;  // sorted keys
 
     Buf aos, pos_in, vel_in, igrp_in, rk_in, keys0, keys1, vals0, vals1, sort_tmp;
     Buf pos, vel, igrp, rk, t33, idx33;
-    Buf meta, parent, leaf_parent, flags, blo, bhi, elo, ehi;
+    Buf meta, parent, leaf_parent, flags, blo, bhi;
+    Buf dacc, dexp;  // dens: fixed-point sums and scale exponents
     Buf uf, minin, mark, scan_tmp, lab_cnt, lab_scan;
     Buf halos, hcount, hmass;
     Buf totals, lohi;
@@ -130,6 +132,7 @@ int device_status(int bits)
     if (bits & ERR_RANGE) return ASG_ERR_RANGE;
     if (bits & ERR_UF) return ASG_ERR_UNIONFIND;
     if (bits & ERR_BADCELL) return ASG_ERR_ARG;
+    if (bits & ERR_CAP) return ASG_ERR_STATE;
     return ASG_OK;
 }
 
@@ -194,8 +197,6 @@ TreeView tree_view(asg_ctx* ctx)
     t.meta = P<int4>(ctx->meta);
     t.blo = P<float4>(ctx->blo);
     t.bhi = P<float4>(ctx->bhi);
-    t.elo = P<float4>(ctx->elo);
-    t.ehi = P<float4>(ctx->ehi);
     return t;
 }
 
@@ -224,8 +225,8 @@ int alloc_set(asg_ctx* ctx, int n)
     r |= grow(ctx, ctx->flags, 4 * M);
     r |= grow(ctx, ctx->blo, 16 * M);
     r |= grow(ctx, ctx->bhi, 16 * M);
-    r |= grow(ctx, ctx->elo, 16 * M);
-    r |= grow(ctx, ctx->ehi, 16 * M);
+    r |= grow(ctx, ctx->dacc, 8 * N);
+    r |= grow(ctx, ctx->dexp, 4 * N);
     return r ? ASG_ERR_NOMEM : 0;
 }
 
@@ -242,13 +243,13 @@ int build_index(asg_ctx* ctx)
                          P<float4>(ctx->vel), P<int>(ctx->igrp), P<float>(ctx->rk), ctx->s);
     launch_build_tree(ctx->keys, n, P<int4>(ctx->meta), P<int>(ctx->parent),
                       P<int>(ctx->leaf_parent), ctx->s);
-    launch_tree_boxes(P<float4>(ctx->pos), nullptr, n, P<int4>(ctx->meta), P<int>(ctx->parent),
-                      P<int>(ctx->leaf_parent), P<int>(ctx->flags), P<float4>(ctx->blo),
+    launch_tree_boxes(P<float4>(ctx->pos), nullptr, n, ctx->leaf, P<int4>(ctx->meta),
+                      P<int>(ctx->parent), P<int>(ctx->flags), P<float4>(ctx->blo),
                       P<float4>(ctx->bhi), ctx->s);
     phase_end(ctx);
     ctx->loaded = true;
     ctx->knn_done = false;
-    ctx->ebox_valid = false;
+    ctx->rk_checked = false;
     return 0;
 }
 
@@ -303,16 +304,14 @@ int stage_quant(asg_ctx* ctx, const int* cell, const uint16_t* off, const float*
     return 0;
 }
 
-int ensure_ebox(asg_ctx* ctx)
+// the smoothing lengths are checked once per neighbour search
+int ensure_rk_checked(asg_ctx* ctx)
 {
-    if (ctx->ebox_valid) return 0;
-    phase_begin(ctx, ASG_PH_BOXES);
+    if (ctx->rk_checked) return 0;
+    phase_begin(ctx, ASG_PH_CHECK);
     launch_check_rk(P<float>(ctx->rk), ctx->n, ctx->d_err, ctx->s);
-    launch_tree_boxes(P<float4>(ctx->pos), P<float>(ctx->rk), ctx->n, P<int4>(ctx->meta),
-                      P<int>(ctx->parent), P<int>(ctx->leaf_parent), P<int>(ctx->flags),
-                      P<float4>(ctx->elo), P<float4>(ctx->ehi), ctx->s);
     phase_end(ctx);
-    ctx->ebox_valid = true;
+    ctx->rk_checked = true;
     return 0;
 }
 
@@ -380,7 +379,7 @@ void asg_destroy(asg_ctx* ctx)
                    &ctx->keys0, &ctx->keys1, &ctx->vals0, &ctx->vals1, &ctx->sort_tmp,
                    &ctx->pos, &ctx->vel, &ctx->igrp, &ctx->rk, &ctx->t33, &ctx->idx33,
                    &ctx->meta, &ctx->parent, &ctx->leaf_parent, &ctx->flags, &ctx->blo,
-                   &ctx->bhi, &ctx->elo, &ctx->ehi, &ctx->uf, &ctx->minin, &ctx->mark,
+                   &ctx->bhi, &ctx->dacc, &ctx->dexp, &ctx->uf, &ctx->minin, &ctx->mark,
                    &ctx->scan_tmp, &ctx->lab_cnt, &ctx->lab_scan, &ctx->halos, &ctx->hcount,
                    &ctx->hmass, &ctx->totals, &ctx->lohi, &ctx->dep_rec, &ctx->dep_pcount,
                    &ctx->dep_tiles, &ctx->dep_counter, &ctx->dep_pairs, &ctx->dep_sort,
@@ -793,11 +792,11 @@ static int run_knn(asg_ctx* ctx)
                     ctx->d_err, ctx->s);
     phase_end(ctx);
     ctx->idx33_all = false;
-    ctx->ebox_valid = false;
-    ensure_ebox(ctx);
+    ctx->rk_checked = false;
+    ensure_rk_checked(ctx);
     phase_begin(ctx, ASG_PH_DENS);
-    launch_dens_gather(P<float4>(ctx->pos), tree_view(ctx), P<float>(ctx->t33), P<int>(ctx->idx33),
-                       P<float>(ctx->rk), P<float4>(ctx->vel), ctx->s);
+    launch_dens(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33), P<float>(ctx->rk),
+                P<int>(ctx->dexp), P<unsigned long long>(ctx->dacc), P<float4>(ctx->vel), ctx->s);
     phase_end(ctx);
     ctx->knn_done = true;
     return 0;
@@ -930,14 +929,16 @@ int asg_run_remove_small_groups(asg_ctx* ctx, int ngrp, int* nhalo)
     return 0;
 }
 
+// cap == 0: size the pair arrays from the pair count (one host synchronisation);
+// cap > 0: pair arrays of that capacity, no synchronisation (stream capture)
 static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,
-                         int periodic, const int* coords, int density_only)
+                         int periodic, const int* coords, int density_only, uint32_t cap = 0)
 {
     if (!ncs || n_nc <= 0 || n_nc > MAX_MESHES) return fail(ctx, ASG_ERR_ARG, "1..8 meshes");
     if (!(boxsize > 0.0f) || !std::isfinite(boxsize)) return fail(ctx, ASG_ERR_ARG, "boxsize");
     for (int k = 0; k < n_nc; ++k)
         if (ncs[k] <= 0 || ncs[k] > 1290) return fail(ctx, ASG_ERR_ARG, "nc out of range");
-    ensure_ebox(ctx);
+    ensure_rk_checked(ctx);
     if ((int)ctx->meshes.size() < n_nc) ctx->meshes.resize((size_t)n_nc);
     ctx->mesh_boxsize = boxsize;
     DepositParams p;
@@ -947,6 +948,7 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     p.sign = sign;
     p.periodic = periodic ? 1 : 0;
     p.density_only = density_only ? 1 : 0;
+    p.seg = ctx->dep_seg;
     for (int d = 0; d < 3; ++d) p.offset[d] = periodic && coords ? boxsize * (float)coords[d] : 0.0f;
     int tiles = 0;
     for (int k = 0; k < n_nc; ++k) {
@@ -989,13 +991,16 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     phase_begin(ctx, ASG_PH_DEPOSIT);
     launch_deposit_prep(P<float4>(ctx->pos), P<float4>(ctx->vel), P<int>(ctx->igrp),
                         P<float>(ctx->rk), n, p, w, ctx->d_err, ctx->s);
-    CK(cudaMemcpyAsync(ctx->h_u32, w.pcount + n, 4, cudaMemcpyDeviceToHost, ctx->s));
-    CK(cudaStreamSynchronize(ctx->s));
-    const uint32_t npairs = ctx->h_u32[0];
+    uint32_t npairs = cap;
+    if (!cap) {
+        CK(cudaMemcpyAsync(ctx->h_u32, w.pcount + n, 4, cudaMemcpyDeviceToHost, ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+        npairs = ctx->h_u32[0];
+    }
     const size_t NP = (size_t)npairs + 1;
     if (int r = grow(ctx, ctx->dep_pairs, 16 * NP)) return r;
     if (int r = grow(ctx, ctx->dep_sort, radix_sort_temp_bytes((int)NP))) return r;
-    const uint32_t max_items = deposit_max_items(tiles, npairs);
+    const uint32_t max_items = deposit_max_items(tiles, npairs, p.seg);
     if (int r = grow(ctx, ctx->dep_partial, deposit_partial_bytes(max_items) + 16)) return r;
     w.keys0 = P<uint32_t>(ctx->dep_pairs);
     w.keys1 = w.keys0 + NP;
@@ -1003,9 +1008,9 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     w.vals1 = w.vals0 + NP;
     w.sort_tmp = ctx->dep_sort.p;
     w.partial = P<float>(ctx->dep_partial);
-    ctx->dep_npairs = npairs;
+    if (!cap) ctx->dep_npairs = npairs;
     ctx->dep_tiles_n = tiles;
-    launch_deposit_run(n, p, tiles, npairs, w, ctx->d_err, ctx->s);
+    launch_deposit_run(n, p, tiles, npairs, cap != 0, w, ctx->d_err, ctx->s);
     for (int k = 0; k < n_nc; ++k) {
         const int tpd = (ncs[k] + 7) / 8;
         launch_reduce_partials(P<double>(ctx->meshes[(size_t)k].partial), tpd * tpd * tpd,
@@ -1319,7 +1324,7 @@ int asg_phase_ms(asg_ctx* ctx, double* ms)
 
 const char* asg_phase_name(int phase)
 {
-    static const char* names[ASG_NPHASES] = {"index", "knn_t33", "knn_ties", "boxes",
+    static const char* names[ASG_NPHASES] = {"index", "knn_t33", "knn_ties", "check_rk",
                                              "dens",  "deposit", "halos",    "fof"};
     return (phase >= 0 && phase < ASG_NPHASES) ? names[phase] : "?";
 }
@@ -1453,6 +1458,308 @@ int asg_smooth_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off, con
     if (totals)
         CK(cudaMemcpyAsync(totals, ctx->totals.p, 16 * (size_t)n_nc, cudaMemcpyDeviceToHost, ctx->s));
     return finish(ctx, "smooth_quantised");
+}
+
+}  // extern "C"
+
+// ---- batched form: many cubes, one CUDA graph ------------------------------------------
+
+struct asg_batch {
+    asg_ctx* ctx = nullptr;
+    int n_items = 0, n_nc = 0, sign = -1;
+    std::vector<int> np, np_local, ncs;
+    std::vector<float> left, right, box;
+    std::vector<size_t> off;       // first particle of each item in the concatenated arrays
+    std::vector<size_t> mesh_off;  // first float of mesh (item, k) in out_mesh
+    size_t n_total = 0, mesh_words = 0;
+    int max_n = 0;
+    Buf in_x, in_v, out_rk, out_dens, out_mesh, out_tot;
+    std::vector<uint32_t> cap;     // pair capacity per item (from the planning pass)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;        // kernels per graph launch
+    double last_ms = 0.0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+namespace {
+
+void batch_drop_graph(asg_batch* b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+// one item's whole path on the context stream; cap = 0 sizes the deposit from
+// its pair count (one synchronisation), cap > 0 synchronises nowhere
+int batch_queue_item(asg_batch* b, int i, uint32_t cap)
+{
+    asg_ctx* ctx = b->ctx;
+    const int n = b->np[(size_t)i];
+    const size_t o = b->off[(size_t)i];
+    ctx->n = n;
+    ctx->left = b->left[(size_t)i];
+    ctx->right = b->right[(size_t)i];
+    launch_unpack_soa(P<float>(b->in_x) + 3 * o, P<float>(b->in_v) + 3 * o, nullptr, nullptr, n,
+                      P<float4>(ctx->pos_in), P<float4>(ctx->vel_in), P<int>(ctx->igrp_in),
+                      P<float>(ctx->rk_in), ctx->d_err, ctx->s);
+    launch_morton(P<float4>(ctx->pos_in), n, ctx->left, ctx->right, nullptr, 0,
+                  P<uint64_t>(ctx->keys0), P<int>(ctx->vals0), ctx->s);
+    build_index(ctx);
+    run_knn(ctx);
+    if (int r = queue_deposit(ctx, b->box[(size_t)i], b->ncs.data(), b->n_nc, b->sign, 0, nullptr, 0,
+                              cap))
+        return r;
+    k_dens_of<<<(n + 255) / 256, 256, 0, ctx->s>>>(P<float4>(ctx->vel), n, P<float>(ctx->lab_scan));
+    count_launches(1);
+    launch_scatter_fields(ctx->perm, P<float>(ctx->rk), P<float>(ctx->lab_scan), nullptr, n,
+                          P<float>(b->out_rk) + o, P<float>(b->out_dens) + o, nullptr, ctx->s);
+    for (int k = 0; k < b->n_nc; ++k) {
+        const MeshBuf& mb = ctx->meshes[(size_t)k];
+        CK(cudaMemcpyAsync(P<float>(b->out_mesh) + b->mesh_off[(size_t)i * b->n_nc + k], mb.mesh.p,
+                           4 * mb.words, cudaMemcpyDeviceToDevice, ctx->s));
+    }
+    CK(cudaMemcpyAsync(P<double>(b->out_tot) + 2 * (size_t)i * b->n_nc, ctx->totals.p,
+                       16 * (size_t)b->n_nc, cudaMemcpyDeviceToDevice, ctx->s));
+    return 0;
+}
+
+// eager pass over every item: sizes every buffer and records each pair count
+int batch_plan(asg_batch* b)
+{
+    asg_ctx* ctx = b->ctx;
+    if (int r = alloc_set(ctx, b->max_n)) return r;
+    if (int r = grow(ctx, ctx->lab_scan, 4 * (size_t)b->max_n)) return r;
+    b->cap.assign((size_t)b->n_items, 0u);
+    uint32_t max_cap = 0;
+    for (int i = 0; i < b->n_items; ++i) {
+        if (int r = batch_queue_item(b, i, 0)) return r;
+        const uint32_t np = ctx->dep_npairs;
+        b->cap[(size_t)i] = np + np / 16 + 4096;  // headroom for inputs that change between runs
+        max_cap = std::max(max_cap, b->cap[(size_t)i]);
+    }
+    if (int r = finish(ctx, "batch plan")) return r;
+    // reserve the deposit arrays for the largest capacity, so that the capture allocates nothing
+    const size_t NP = (size_t)max_cap + 1;
+    if (int r = grow(ctx, ctx->dep_pairs, 16 * NP)) return r;
+    if (int r = grow(ctx, ctx->dep_sort, radix_sort_temp_bytes((int)NP))) return r;
+    const uint32_t items = deposit_max_items(ctx->dep_tiles_n, max_cap, ctx->dep_seg);
+    return grow(ctx, ctx->dep_partial, deposit_partial_bytes(items) + 16);
+}
+
+int batch_capture(asg_batch* b)
+{
+    asg_ctx* ctx = b->ctx;
+    batch_drop_graph(b);
+    const bool timing = ctx->timing;
+    ctx->timing = false;
+    const long long l0 = g_launches.load();
+    cudaError_t e = cudaStreamBeginCapture(ctx->s, cudaStreamCaptureModeThreadLocal);
+    int r = e == cudaSuccess ? 0 : cuda_fail(ctx, e, "cudaStreamBeginCapture");
+    for (int i = 0; !r && i < b->n_items; ++i) r = batch_queue_item(b, i, b->cap[(size_t)i]);
+    cudaGraph_t g = nullptr;
+    if (e == cudaSuccess) {
+        const cudaError_t e2 = cudaStreamEndCapture(ctx->s, &g);
+        if (!r && e2 != cudaSuccess) r = cuda_fail(ctx, e2, "cudaStreamEndCapture");
+    }
+    ctx->timing = timing;
+    b->launches = g_launches.load() - l0;
+    if (r) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return r;
+    }
+    b->graph = g;
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (e != cudaSuccess) {
+        batch_drop_graph(b);
+        return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int asg_batch_create(asg_ctx* ctx, int n_items, const int* np, const int* np_local,
+                     const float* left, const float* right, const float* boxsize, const int* ncs,
+                     int n_nc, int sign, asg_batch** out)
+{
+    if (!ctx || !out || n_items <= 0 || !np || !left || !right || !boxsize || !ncs || n_nc <= 0 ||
+        n_nc > MAX_MESHES)
+        return fail(ctx, ASG_ERR_ARG, "bad arguments");
+    *out = nullptr;
+    for (int k = 0; k < n_nc; ++k)
+        if (ncs[k] <= 0 || ncs[k] > 1290) return fail(ctx, ASG_ERR_ARG, "nc out of range");
+    CK(cudaSetDevice(ctx->device));
+    asg_batch* b = new asg_batch();
+    b->ctx = ctx;
+    b->n_items = n_items;
+    b->n_nc = n_nc;
+    b->sign = sign;
+    b->ncs.assign(ncs, ncs + n_nc);
+    size_t mw = 0;
+    for (int i = 0; i < n_items; ++i) {
+        if (np[i] < K_NN || !(left[i] < right[i]) || !(boxsize[i] > 0.0f)) {
+            delete b;
+            return fail(ctx, ASG_ERR_ARG, "item " + std::to_string(i) + ": bad size or bounds");
+        }
+        b->np.push_back(np[i]);
+        b->np_local.push_back(np_local ? np_local[i] : np[i]);
+        b->left.push_back(left[i]);
+        b->right.push_back(right[i]);
+        b->box.push_back(boxsize[i]);
+        b->off.push_back(b->n_total);
+        b->n_total += (size_t)np[i];
+        b->max_n = std::max(b->max_n, np[i]);
+        for (int k = 0; k < n_nc; ++k) {
+            b->mesh_off.push_back(mw);
+            mw += 6 * (size_t)ncs[k] * ncs[k] * ncs[k];
+        }
+    }
+    b->mesh_words = mw;
+    int r = grow(ctx, b->in_x, 12 * b->n_total);
+    if (!r) r = grow(ctx, b->in_v, 12 * b->n_total);
+    if (!r) r = grow(ctx, b->out_rk, 4 * b->n_total);
+    if (!r) r = grow(ctx, b->out_dens, 4 * b->n_total);
+    if (!r) r = grow(ctx, b->out_mesh, 4 * mw);
+    if (!r) r = grow(ctx, b->out_tot, 16 * (size_t)n_items * n_nc);
+    if (!r && (cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess))
+        r = fail(ctx, ASG_ERR_CUDA, "cudaEventCreate");
+    if (!r) r = cudaMemsetAsync(b->in_v.p, 0, 12 * b->n_total, ctx->s) == cudaSuccess
+                    ? 0 : fail(ctx, ASG_ERR_CUDA, "memset");
+    if (r) {
+        asg_batch_destroy(b);
+        return r;
+    }
+    *out = b;
+    return ASG_OK;
+}
+
+void asg_batch_destroy(asg_batch* b)
+{
+    if (!b) return;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->s);
+    batch_drop_graph(b);
+    for (Buf* x : {&b->in_x, &b->in_v, &b->out_rk, &b->out_dens, &b->out_mesh, &b->out_tot})
+        if (x->p) cudaFree(x->p);
+    if (b->e0) cudaEventDestroy(b->e0);
+    if (b->e1) cudaEventDestroy(b->e1);
+    delete b;
+}
+
+int asg_batch_set_item(asg_batch* b, int item, const float* x, const float* v, int device_ptrs)
+{
+    if (!b || !x || item < 0 || item >= b->n_items) return ASG_ERR_ARG;
+    asg_ctx* ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device));
+    const size_t o = b->off[(size_t)item], bytes = 12 * (size_t)b->np[(size_t)item];
+    const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    CK(cudaMemcpyAsync(P<float>(b->in_x) + 3 * o, x, bytes, kind, ctx->s));
+    if (v) CK(cudaMemcpyAsync(P<float>(b->in_v) + 3 * o, v, bytes, kind, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return ASG_OK;
+}
+
+int asg_batch_tune(asg_batch* b, int* leaf, int* seg)
+{
+    if (!b) return ASG_ERR_ARG;
+    asg_ctx* ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device));
+    if (int r = alloc_set(ctx, b->max_n)) return r;
+    if (int r = grow(ctx, ctx->lab_scan, 4 * (size_t)b->max_n)) return r;
+    int item = 0;  // the largest item
+    for (int i = 1; i < b->n_items; ++i)
+        if (b->np[(size_t)i] > b->np[(size_t)item]) item = i;
+    const int leaves[] = {16, 24, 32}, segs[] = {2048, 4096, 8192};
+    float best = INFINITY;
+    int bl = ctx->leaf, bs = ctx->dep_seg;
+    for (int l : leaves)
+        for (int s : segs) {
+            ctx->leaf = l;
+            ctx->dep_seg = s;
+            float ms = 0.0f;
+            for (int rep = 0; rep < 2; ++rep) {  // the first repetition warms up
+                CK(cudaEventRecord(b->e0, ctx->s));
+                if (int r = batch_queue_item(b, item, 0)) return r;
+                CK(cudaEventRecord(b->e1, ctx->s));
+                CK(cudaEventSynchronize(b->e1));
+                CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
+            }
+            if (ms < best) {
+                best = ms;
+                bl = l;
+                bs = s;
+            }
+        }
+    ctx->leaf = bl;
+    ctx->dep_seg = bs;
+    batch_drop_graph(b);  // a new configuration needs a new plan and capture
+    if (leaf) *leaf = bl;
+    if (seg) *seg = bs;
+    return finish(ctx, "batch tune");
+}
+
+int asg_batch_run(asg_batch* b)
+{
+    if (!b) return ASG_ERR_ARG;
+    asg_ctx* ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device));
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (!b->exec) {
+            if (int r = batch_plan(b)) return r;
+            if (int r = batch_capture(b)) return r;
+        }
+        CK(cudaEventRecord(b->e0, ctx->s));
+        CK(cudaGraphLaunch(b->exec, ctx->s));
+        CK(cudaEventRecord(b->e1, ctx->s));
+        count_launches((int)b->launches);
+        const int r = finish(ctx, "batch run");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, b->e0, b->e1) == cudaSuccess) b->last_ms = ms;
+        if (r != ASG_ERR_STATE) return r;  // ERR_CAP: the inputs outgrew the plan
+        batch_drop_graph(b);
+    }
+    return fail(ctx, ASG_ERR_STATE, "batch: pair capacity exceeded twice");
+}
+
+int asg_batch_stats(asg_batch* b, double* graph_ms, long long* kernels, long long* particles_local)
+{
+    if (!b) return ASG_ERR_ARG;
+    if (graph_ms) *graph_ms = b->last_ms;
+    if (kernels) *kernels = b->launches;
+    if (particles_local) {
+        long long s = 0;
+        for (int v : b->np_local) s += v;
+        *particles_local = s;
+    }
+    return ASG_OK;
+}
+
+int asg_batch_get(asg_batch* b, int item, float* rk, float* dens, float* const* meshes,
+                  double* totals)
+{
+    if (!b || item < 0 || item >= b->n_items) return ASG_ERR_ARG;
+    asg_ctx* ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device));
+    const size_t o = b->off[(size_t)item], n = (size_t)b->np[(size_t)item];
+    if (rk) CK(cudaMemcpyAsync(rk, P<float>(b->out_rk) + o, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
+    if (dens) CK(cudaMemcpyAsync(dens, P<float>(b->out_dens) + o, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
+    for (int k = 0; meshes && k < b->n_nc; ++k)
+        if (meshes[k]) {
+            const size_t nc = (size_t)b->ncs[(size_t)k];
+            CK(cudaMemcpyAsync(meshes[k], P<float>(b->out_mesh) + b->mesh_off[(size_t)item * b->n_nc + k],
+                               24 * nc * nc * nc, cudaMemcpyDeviceToHost, ctx->s));
+        }
+    if (totals)
+        CK(cudaMemcpyAsync(totals, P<double>(b->out_tot) + 2 * (size_t)item * b->n_nc,
+                           16 * (size_t)b->n_nc, cudaMemcpyDeviceToHost, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return ASG_OK;
 }
 
 }  // extern "C"

@@ -26,6 +26,7 @@ constexpr int ERR_NONFINITE = 16;  // NaN / inf position
 constexpr int ERR_UF = 32;         // union-find retry limit hit
 constexpr int ERR_RANGE = 64;      // periodic deposit range wider than the mesh
 constexpr int ERR_BADCELL = 128;   // mixed-precision cell index outside the grid
+constexpr int ERR_CAP = 256;       // more deposit pairs than a pre-sized pair array holds
 
 // ---- exact float helpers (reference expression order) ----------------------
 
@@ -72,6 +73,18 @@ __device__ __forceinline__ float box_dist2_rn(float qx, float qy, float qz, floa
 }
 
 // double-float accumulation (Knuth two-sum): hi + lo carries ~48 bits
+// the same (hi, lo) as two_sum_acc for hi >= 0 and x >= 0: Fast2Sum on the
+// larger and the smaller operand gives the same rounded sum and the same exact
+// error, with a shorter dependency chain
+__device__ __forceinline__ void two_sum_acc_nonneg(float& hi, float& lo, float x)
+{
+    const float a = fmaxf(hi, x), b = fminf(hi, x);
+    const float s = __fadd_rn(a, b);
+    const float e = __fsub_rn(b, __fsub_rn(s, a));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x)
 {
     const float s = __fadd_rn(hi, x);

@@ -19,7 +19,7 @@
 //  (3) a stable radix sort of the pairs by key = tile << 5 | image groups each
 //      tile's particles in particle order.
 //  (4) k_deposit_items: a persistent kernel whose warps take (tile, segment
-//      of SEG pairs) work items; a warp accumulates its item in a private
+//      of seg pairs) work items; a warp accumulates its item in a private
 //      shared-memory tile and adds one pair after another, its lanes over the
 //      pair's 3-D cell box, so every cell sums its contributions in list
 //      order.  k_merge_tiles adds the partial tiles of multi-segment tiles in
@@ -34,7 +34,7 @@ namespace asg {
 constexpr int TS = 8;              // tile edge in cells
 constexpr int TC = TS * TS * TS;   // cells per tile
 constexpr int DEP_THREADS = 256;   // threads of the tile-merge CTA
-constexpr int SEG = 4096;          // pairs per work item
+constexpr int SEG_DEFAULT = 4096;  // pairs per work item unless DepositParams::seg says otherwise
 constexpr int PW = 9;              // partial words per cell
 constexpr int IMG_BITS = 5;        // periodic images per pair: up to 3 x 3 x 3
 constexpr unsigned FULLM = 0xffffffffu;
@@ -139,10 +139,12 @@ __device__ __forceinline__ void image_tiles(const AxisRange& r, int k, int nc, i
     t1 = c1 > c0 ? (c1 - 1) / TS : t0 - 1;
 }
 
+// EMIT writes pair o only when o < cap (the pair arrays' capacity); a pair
+// beyond it sets ERR_CAP instead
 template <bool EMIT>
 __global__ void k_pairs(const float4* __restrict__ rec, int n, DepositParams P,
                         uint32_t* __restrict__ counts, const uint32_t* __restrict__ offs,
-                        uint32_t* __restrict__ keys, int* __restrict__ vals, int* err)
+                        uint32_t* __restrict__ keys, int* __restrict__ vals, uint32_t cap, int* err)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -183,8 +185,12 @@ __global__ void k_pairs(const float4* __restrict__ rec, int n, DepositParams P,
                                     for (int tx = x0; tx <= x1; ++tx) {
                                         const uint32_t tile = (uint32_t)J.tile_begin +
                                             (uint32_t)((tz * J.tiles[1] + ty) * J.tiles[0] + tx);
-                                        keys[o] = (tile << IMG_BITS) | combo;
-                                        vals[o] = i;
+                                        if (o < cap) {
+                                            keys[o] = (tile << IMG_BITS) | combo;
+                                            vals[o] = i;
+                                        } else {
+                                            atomicOr(err, ERR_CAP);
+                                        }
                                         ++o;
                                     }
                         }
@@ -196,26 +202,39 @@ __global__ void k_pairs(const float4* __restrict__ rec, int n, DepositParams P,
     if (!EMIT) counts[i] = cnt;
 }
 
-// first pair and pair count of every tile (sorted keys; empty tiles stay 0)
-__global__ void k_tile_bounds(const uint32_t* __restrict__ keys, int np, uint32_t* __restrict__ tstart,
-                              uint32_t* __restrict__ tcount)
+// pairs [*npairs, cap) of a pre-sized pair array: key of tile T (past the last
+// real tile), so they sort last and k_tile_bounds skips them
+__global__ void k_pad_pairs(uint32_t* __restrict__ keys, int* __restrict__ vals,
+                            const uint32_t* __restrict__ npairs, uint32_t cap, uint32_t pad_key)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cap || j < *npairs) return;
+    keys[j] = pad_key;
+    vals[j] = 0;
+}
+
+// first pair and pair count of every tile (sorted keys; empty tiles stay 0;
+// tiles >= total_tiles are padding)
+__global__ void k_tile_bounds(const uint32_t* __restrict__ keys, int np, int total_tiles,
+                              uint32_t* __restrict__ tstart, uint32_t* __restrict__ tcount)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= np) return;
     const uint32_t t = keys[j] >> IMG_BITS;
+    if (t >= (uint32_t)total_tiles) return;
     if (j == 0 || (keys[j - 1] >> IMG_BITS) != t) tstart[t] = (uint32_t)j;
     if (j == np - 1 || (keys[j + 1] >> IMG_BITS) != t) tcount[t] = (uint32_t)j + 1;  // end for now
 }
 
-// tcount: end -> count; nitems: SEG-pair work items per tile (at least one)
+// tcount: end -> count; nitems: seg-pair work items per tile (at least one)
 __global__ void k_tile_items(const uint32_t* __restrict__ tstart, uint32_t* __restrict__ tcount,
-                             int total_tiles, uint32_t* __restrict__ nitems)
+                             int total_tiles, int seg, uint32_t* __restrict__ nitems)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < total_tiles) {
         const uint32_t c = tcount[i] ? tcount[i] - tstart[i] : 0u;
         tcount[i] = c;
-        nitems[i] = max(1u, (c + SEG - 1) / SEG);
+        nitems[i] = max(1u, (c + (uint32_t)seg - 1) / (uint32_t)seg);
     }
     if (i == total_tiles) nitems[i] = 0u;
 }
@@ -257,6 +276,33 @@ __constant__ float c_rcp[TS * TS + 1] = {0.0f, ASG_R8(0), ASG_R8(8), ASG_R8(16),
 __device__ __forceinline__ int small_div(int c, float rcp)
 {
     return __float2int_rz(__fmul_rn(__fadd_rn(__int2float_rn(c), 0.5f), rcp));
+}
+
+// one particle's weight w3 into one cell: n and c as double-float, v as float
+__device__ __forceinline__ void add_cell(WarpTile& S, int slot, float w3, float dens, float vx,
+                                         float vy, float vz)
+{
+    float4 Aa = S.a[slot];
+    float4 Bb = S.b[slot];
+    two_sum_acc_nonneg(Aa.x, Aa.y, w3);
+    const float pr = __fmul_rn(w3, dens);
+    const float pe = fmaf(w3, dens, -pr);  // the exact rounding error of the product
+    two_sum_acc_nonneg(Aa.z, Aa.w, pr);
+    Aa.w = __fadd_rn(Aa.w, pe);
+    Bb.x = fmaf(w3, vx, Bb.x);
+    Bb.y = fmaf(w3, vy, Bb.y);
+    Bb.z = fmaf(w3, vz, Bb.z);
+    S.a[slot] = Aa;
+    S.b[slot] = Bb;
+}
+
+// a halo particle's weight into the halo channel (double-float)
+__device__ __forceinline__ void add_halo(WarpTile& S, int slot, float w3)
+{
+    float hh = S.b[slot].w, hl = S.hl[slot];
+    two_sum_acc_nonneg(hh, hl, w3);
+    S.b[slot].w = hh;
+    S.hl[slot] = hl;
 }
 
 __device__ __forceinline__ int upper_index(const uint32_t* __restrict__ a, int n, uint32_t v)
@@ -349,8 +395,8 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
         const int nc = g.nc;
         const int seg = item - (int)item_off[tile];
         const int nseg = (int)(item_off[tile + 1] - item_off[tile]);
-        const int j0 = (int)tstart[tile] + seg * SEG;
-        const int j1 = (int)tstart[tile] + min((int)tcount[tile], (seg + 1) * SEG);
+        const int j0 = (int)tstart[tile] + seg * P.seg;
+        const int j1 = (int)tstart[tile] + min((int)tcount[tile], (seg + 1) * P.seg);
 
         for (int e = lane; e < TC; e += 32) {
             S.a[e] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -415,26 +461,36 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                 const int nxy = nx * ny, ncell = nxy * nz;
                 const float rx = c_rcp[nx], rxy = c_rcp[nxy];
                 const float* wp = S.w[p];
-                if (!(rp >> 24)) {
+                const bool hal = (rp >> 24) != 0;
+                // column mapping when it needs no more passes than the packed one
+                const int lpi = nxy <= 32 ? small_div(32, rxy) : 0;
+                const bool columns =
+                    lpi > 0 && small_div(nz + lpi - 1, c_rcp[lpi]) <= ((ncell + 31) >> 5);
+                if (columns) {
+                    // each lane owns one (x, y) column and steps through z: lpi
+                    // layers of nx*ny lanes per pass; (wx*wy) once per pair
+                    const int lz = small_div(lane, rxy);
+                    const int r = lane - lz * nxy;
+                    const int ly = small_div(r, rx);
+                    const int gx = x0 + r - ly * nx, gy = y0 + ly;
+                    if (lz < lpi) {
+                        const float wxy = __fmul_rn(wp[gx], wp[TS + gy]);
+                        const int sb = gy << 3, xr = gx + 6 * gy;
+                        for (int gz = z0 + lz; gz < z0 + nz; gz += lpi) {
+                            const float w3 = __fmul_rn(wxy, wp[2 * TS + gz]);
+                            const int slot = (gz << 6) | sb | ((xr + 4 * gz) & (TS - 1));
+                            if (!hal) add_cell(S, slot, w3, dens, vx, vy, vz);
+                            else add_halo(S, slot, w3);
+                        }
+                    }
+                } else if (!hal) {
                     for (int c = lane; c < ncell; c += 32) {
                         const int iz = small_div(c, rxy);
                         const int rem = c - iz * nxy;
                         const int iy = small_div(rem, rx);
                         const int gx = x0 + rem - iy * nx, gy = y0 + iy, gz = z0 + iz;
                         const float w3 = __fmul_rn(__fmul_rn(wp[gx], wp[TS + gy]), wp[2 * TS + gz]);
-                        const int slot = tile_slot(gx, gy, gz);
-                        float4 Aa = S.a[slot];
-                        float4 Bb = S.b[slot];
-                        two_sum_acc(Aa.x, Aa.y, w3);
-                        const float pr = __fmul_rn(w3, dens);
-                        const float pe = fmaf(w3, dens, -pr);
-                        two_sum_acc(Aa.z, Aa.w, pr);
-                        Aa.w = __fadd_rn(Aa.w, pe);
-                        Bb.x = fmaf(w3, vx, Bb.x);
-                        Bb.y = fmaf(w3, vy, Bb.y);
-                        Bb.z = fmaf(w3, vz, Bb.z);
-                        S.a[slot] = Aa;
-                        S.b[slot] = Bb;
+                        add_cell(S, tile_slot(gx, gy, gz), w3, dens, vx, vy, vz);
                     }
                 } else {
                     for (int c = lane; c < ncell; c += 32) {
@@ -443,11 +499,7 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                         const int iy = small_div(rem, rx);
                         const int gx = x0 + rem - iy * nx, gy = y0 + iy, gz = z0 + iz;
                         const float w3 = __fmul_rn(__fmul_rn(wp[gx], wp[TS + gy]), wp[2 * TS + gz]);
-                        const int slot = tile_slot(gx, gy, gz);
-                        float hh = S.b[slot].w, hl = S.hl[slot];
-                        two_sum_acc(hh, hl, w3);
-                        S.b[slot].w = hh;
-                        S.hl[slot] = hl;
+                        add_halo(S, tile_slot(gx, gy, gz), w3);
                     }
                 }
                 __syncwarp();  // the next pair may add to the same cells from other lanes
@@ -557,30 +609,35 @@ void launch_deposit_prep(const float4* pos, const float4* vel, const int* igrp, 
 {
     const int nb = (n + 255) / 256;
     k_dep_prep<<<nb, 256, 0, s>>>(pos, vel, igrp, rk, n, p, w.rec, err);
-    k_pairs<false><<<nb, 256, 0, s>>>(w.rec, n, p, w.pcount, nullptr, nullptr, nullptr, err);
+    k_pairs<false><<<nb, 256, 0, s>>>(w.rec, n, p, w.pcount, nullptr, nullptr, nullptr, 0u, err);
     cudaMemsetAsync(w.pcount + n, 0, 4, s);
     exclusive_scan_u32(w.pcount, (size_t)n + 1, w.scan_tmp_n, s);
     count_launches(2);
 }
 
-void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t npairs,
+void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t npairs, bool padded,
                         DepositScratch& w, int* err, cudaStream_t s)
 {
     const int T = total_tiles;
     const int nb = (n + 255) / 256;
-    k_pairs<true><<<nb, 256, 0, s>>>(w.rec, n, p, nullptr, w.pcount, w.keys0, w.vals0, err);
+    k_pairs<true><<<nb, 256, 0, s>>>(w.rec, n, p, nullptr, w.pcount, w.keys0, w.vals0, npairs, err);
     count_launches(1);
-    const int cur = radix_sort32(w.keys0, w.vals0, w.keys1, w.vals1, (int)npairs, key_bits(T),
-                                 w.sort_tmp, s);
+    if (padded && npairs > 0) {  // npairs is the capacity; the count itself is pcount[n]
+        k_pad_pairs<<<(npairs + 255) / 256, 256, 0, s>>>(w.keys0, w.vals0, w.pcount + n, npairs,
+                                                          (uint32_t)T << IMG_BITS);
+        count_launches(1);
+    }
+    const int cur = radix_sort32(w.keys0, w.vals0, w.keys1, w.vals1, (int)npairs,
+                                 key_bits(padded ? T + 1 : T), w.sort_tmp, s);
     const uint32_t* keys = cur ? w.keys1 : w.keys0;
     const int* vals = cur ? w.vals1 : w.vals0;
     cudaMemsetAsync(w.tstart, 0, 4 * (size_t)T, s);
     cudaMemsetAsync(w.tcount, 0, 4 * (size_t)T, s);
     if (npairs > 0) {
-        k_tile_bounds<<<(npairs + 255) / 256, 256, 0, s>>>(keys, (int)npairs, w.tstart, w.tcount);
+        k_tile_bounds<<<(npairs + 255) / 256, 256, 0, s>>>(keys, (int)npairs, T, w.tstart, w.tcount);
         count_launches(1);
     }
-    k_tile_items<<<(T + 1 + 255) / 256, 256, 0, s>>>(w.tstart, w.tcount, T, w.item_off);
+    k_tile_items<<<(T + 1 + 255) / 256, 256, 0, s>>>(w.tstart, w.tcount, T, p.seg, w.item_off);
     exclusive_scan_u32(w.item_off, (size_t)T + 1, w.scan_tmp_t, s);
     cudaMemsetAsync(w.next_item, 0, sizeof(int), s);
     const size_t smem = DEP_WARPS * sizeof(WarpTile);
@@ -601,10 +658,12 @@ void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t
     count_launches(3);
 }
 
-uint32_t deposit_max_items(int total_tiles, uint32_t npairs)
+uint32_t deposit_max_items(int total_tiles, uint32_t npairs, int seg)
 {
-    return (uint32_t)total_tiles + npairs / SEG + 1;
+    return (uint32_t)total_tiles + npairs / (uint32_t)(seg > 0 ? seg : SEG_DEFAULT) + 1;
 }
+
+int deposit_default_seg() { return SEG_DEFAULT; }
 
 size_t deposit_partial_bytes(uint32_t items) { return (size_t)items * TC * PW * sizeof(float); }
 

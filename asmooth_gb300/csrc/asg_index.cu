@@ -503,38 +503,71 @@ __device__ __forceinline__ void leaf_box(const float4* pos, const float* rk, int
     }
 }
 
+__device__ __forceinline__ void box_union(float4& l, float4& h, const float4& l1, const float4& h1)
+{
+    l = make_float4(fminf(l.x, l1.x), fminf(l.y, l1.y), fminf(l.z, l1.z), 0.f);
+    h = make_float4(fmaxf(h.x, h1.x), fmaxf(h.y, h1.y), fmaxf(h.z, h1.z), 0.f);
+}
+
+// Boxes of the nodes a traversal can read: the root and every child of a node
+// with more than `leaf` particles (the traversals scan smaller nodes whole and
+// never look below them).  A "top bucket" (<= leaf particles, parent larger)
+// reduces its contiguous particles directly, then climbs: a node with two
+// internal children is finished by the second arrival (atomic flag), a node
+// with one internal child by its only climber.  Unions of the same particle
+// boxes, so the boxes are the same bits as a climb from every particle.
 __global__ void k_tree_boxes(const float4* __restrict__ pos, const float* __restrict__ rk, int n,
-                             const int4* __restrict__ meta, const int* __restrict__ parent,
-                             const int* __restrict__ leaf_parent, int* flags, float4* lo,
-                             float4* hi)
+                             int leaf, const int4* __restrict__ meta, const int* __restrict__ parent,
+                             int* flags, float4* lo, float4* hi)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int node = leaf_parent[i];
+    if (i >= n - 1) return;
+    const int4 m = meta[i];
+    float4 l, h, l1, h1;
+    if (m.w - m.z + 1 > leaf) {
+        if (m.x >= 0 || m.y >= 0) return;  // reached by the climbs from its internal children
+        leaf_box(pos, rk, ~m.x, l, h);     // two particle children (leaf = 1 only)
+        leaf_box(pos, rk, ~m.y, l1, h1);
+        box_union(l, h, l1, h1);
+    } else {
+        const int p = parent[i];
+        if (p >= 0) {
+            const int4 mp = meta[p];
+            if (mp.w - mp.z + 1 <= leaf) return;  // inside a bucket: never read
+        }
+        leaf_box(pos, rk, m.z, l, h);
+        for (int k = m.z + 1; k <= m.w; ++k) {
+            leaf_box(pos, rk, k, l1, h1);
+            box_union(l, h, l1, h1);
+        }
+    }
+    __stcg(&lo[i], l);
+    __stcg(&hi[i], h);
+    int node = parent[i];
     while (node >= 0) {
-        __threadfence();
-        if (atomicAdd(&flags[node], 1) == 0) return;  // the sibling finishes this node
-        __threadfence();
-        const int4 m = meta[node];
-        float4 l0, h0, l1, h1;
-        if (m.x < 0) leaf_box(pos, rk, ~m.x, l0, h0);
-        else { l0 = __ldcg(&lo[m.x]); h0 = __ldcg(&hi[m.x]); }
-        if (m.y < 0) leaf_box(pos, rk, ~m.y, l1, h1);
-        else { l1 = __ldcg(&lo[m.y]); h1 = __ldcg(&hi[m.y]); }
-        __stcg(&lo[node], make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.f));
-        __stcg(&hi[node], make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.f));
+        const int4 mm = meta[node];
+        if (mm.x >= 0 && mm.y >= 0) {
+            __threadfence();
+            if (atomicAdd(&flags[node], 1) == 0) return;  // the sibling finishes this node
+            __threadfence();
+        }
+        if (mm.x < 0) leaf_box(pos, rk, ~mm.x, l, h);
+        else { l = __ldcg(&lo[mm.x]); h = __ldcg(&hi[mm.x]); }
+        if (mm.y < 0) leaf_box(pos, rk, ~mm.y, l1, h1);
+        else { l1 = __ldcg(&lo[mm.y]); h1 = __ldcg(&hi[mm.y]); }
+        box_union(l, h, l1, h1);
+        __stcg(&lo[node], l);
+        __stcg(&hi[node], h);
         node = parent[node];
     }
 }
 
-void launch_tree_boxes(const float4* pos, const float* rk, int n, const int4* meta,
-                       const int* parent, const int* leaf_parent, int* flags, float4* lo,
-                       float4* hi, cudaStream_t s)
+void launch_tree_boxes(const float4* pos, const float* rk, int n, int leaf, const int4* meta,
+                       const int* parent, int* flags, float4* lo, float4* hi, cudaStream_t s)
 {
     if (n <= 1) return;
     cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(n - 1), s);
-    k_tree_boxes<<<(n + 255) / 256, 256, 0, s>>>(pos, rk, n, meta, parent, leaf_parent, flags, lo,
-                                                  hi);
+    k_tree_boxes<<<(n - 1 + 255) / 256, 256, 0, s>>>(pos, rk, n, leaf, meta, parent, flags, lo, hi);
     count_launches(1);
 }
 

@@ -27,8 +27,6 @@ struct TreeView {
     const int4* meta;      // internal nodes 0..n-2 (root 0); empty when n == 1
     const float4* blo;
     const float4* bhi;
-    const float4* elo;
-    const float4* ehi;
 };
 
 // root entry of a traversal: internal node 0, or leaf 0 when n == 1
@@ -66,10 +64,11 @@ void launch_iota(int* a, int n, cudaStream_t s);
 void launch_check_rk(const float* rk, int n, int* err, cudaStream_t s);
 void launch_build_tree(const uint64_t* keys, int n, int4* meta, int* parent, int* leaf_parent,
                        cudaStream_t s);
-// bottom-up AABBs; with rk != nullptr also the expanded boxes [x-h', x+h']
-void launch_tree_boxes(const float4* pos, const float* rk, int n, const int4* meta,
-                       const int* parent, const int* leaf_parent, int* flags, float4* lo,
-                       float4* hi, cudaStream_t s);
+// bottom-up AABBs of the nodes a traversal with bucket size `leaf` reads (the
+// root and the children of nodes with more than leaf particles); with
+// rk != nullptr the expanded boxes [x-h', x+h']
+void launch_tree_boxes(const float4* pos, const float* rk, int n, int leaf, const int4* meta,
+                       const int* parent, int* flags, float4* lo, float4* hi, cudaStream_t s);
 // exclusive scan of uint32 counts (in place); temp from scan_temp_bytes
 size_t scan_temp_bytes(size_t n);
 void exclusive_scan_u32(uint32_t* data, size_t n, void* temp, cudaStream_t s);
@@ -81,9 +80,10 @@ void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, float* rk,
 // idx33 = input index of the 33rd key, for flagged queries (all = 0) or every query
 void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int* idx33,
                      int all, int* err, cudaStream_t s);
-// vel[j].w (dens) += the tent weights j receives as one of the 32 nearest
-void launch_dens_gather(const float4* pos, const TreeView& t, const float* t33,
-                        const int* idx33, const float* rk, float4* vel, cudaStream_t s);
+// vel[j].w (dens) += the tent weights j receives as one of the 32 nearest;
+// dexp (n ints) and acc (n uint64) are scratch
+void launch_dens(const float4* pos, const TreeView& t, const float* t33, const int* idx33,
+                 const float* rk, int* dexp, unsigned long long* acc, float4* vel, cudaStream_t s);
 
 // ---- mesh deposit (asg_deposit.cu) ---------------------------------------------
 struct MeshJob {
@@ -104,6 +104,7 @@ struct DepositParams {
     int periodic;
     float offset[3];  // periodic: rank cube offset
     int density_only;
+    int seg;          // pairs per work item of the persistent deposit (tuning, > 0)
 };
 // scratch of one deposit: particle records, (tile, image) pairs, work items
 struct DepositScratch {
@@ -124,14 +125,18 @@ struct DepositScratch {
 };
 size_t deposit_prep_bytes(int n);
 size_t deposit_tile_bytes(int total_tiles);
-uint32_t deposit_max_items(int total_tiles, uint32_t npairs);
+uint32_t deposit_max_items(int total_tiles, uint32_t npairs, int seg);
+int deposit_default_seg();
 size_t deposit_partial_bytes(uint32_t items);
 // pass 1: particle records and pair counts; pcount[n] then holds the number of pairs
 void launch_deposit_prep(const float4* pos, const float4* vel, const int* igrp, const float* rk,
                          int n, const DepositParams& p, DepositScratch& w, int* err,
                          cudaStream_t s);
-// pass 2: emit and sort the pairs, deposit every (tile, segment), merge multi-segment tiles
-void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t npairs,
+// pass 2: emit and sort the pairs, deposit every (tile, segment), merge multi-segment tiles.
+// padded = false: npairs is the exact pair count (read back from pcount[n]);
+// padded = true: npairs is the arrays' capacity, the count stays on the device
+// (no host synchronisation, e.g. under stream capture) and a larger count sets ERR_CAP
+void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t npairs, bool padded,
                         DepositScratch& w, int* err, cudaStream_t s);
 void launch_reduce_partials(const double* partial, int ntiles, double* out2, cudaStream_t s);
 void launch_normalise(float* mesh, int nc, float vol, cudaStream_t s);

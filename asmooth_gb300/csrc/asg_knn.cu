@@ -15,9 +15,10 @@
 //               -> t33 = 33rd smallest d2 (exact, with multiplicity)
 //   k_knn_ties  exact-radius recount: L = #(d2 < t33), the tied indices
 //               -> idx33 = input index of the 33rd key, rk = sqrtf(t33)
-//   k_dens_gather  each lane is a RECEIVER j and sums ker(q, j) over the
-//               sources q whose 32-set contains j, in traversal order with a
-//               double-float accumulator: deterministic, no atomics.
+//   k_dens_scatter each lane is a SOURCE q with its exact radius and adds
+//               ker(q, j) to every j of its 32-set as 64-bit fixed point
+//               (per-receiver power-of-two scale, warp-aggregated integer
+//               atomics): exact integer sums, so deterministic in any order.
 #include <climits>
 
 #include "asg_common.cuh"
@@ -234,36 +235,49 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
     }
 }
 
+// dens is summed exactly, in any order, as 64-bit fixed point per receiver j:
+// a weight w is stored as w * 2^(FIX_BITS - e_j), where 2^e_j bounds
+// hinv_j^3.  A query q that has j in its 32-set has rk_j <= 2 rk_q (its 33
+// nearest lie within 2 rk_q of j), so w <= hinv_q^3 <= 8 hinv_j^3 and every
+// term stays below 2^(FIX_BITS + 3 + a rounding margin); the sum of a
+// receiver's terms is exact and independent of the order of the atomic adds.
+constexpr int FIX_BITS = 40;
+
+// e_j with hinv_j^3 < 2^e_j (hinv^3 as the first factor of ker_rn); acc zeroed
+__global__ void k_dens_prep(const float* __restrict__ rk, int n, int* __restrict__ dexp,
+                            unsigned long long* __restrict__ acc)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const float hinv = __fdiv_rn(1.0f, rk[j]);
+    const float h3 = __fmul_rn(__fmul_rn(hinv, hinv), hinv);
+    const int e = ((__float_as_int(h3) >> 23) & 0xff) - 127 + 1;
+    dexp[j] = max(-86, min(86, e));
+    acc[j] = 0ull;
+}
+
+// Each lane is a query q with its exact radius: it visits the candidates j
+// with d2 <= t33_q (the exact-radius traversal of k_knn_ties), and for every j
+// of its 32-set (d2 < t33, or d2 == t33 with index below idx33) the warp adds
+// the members' fixed-point weights and one lane adds the sum to acc[j].
 __global__ void __launch_bounds__(KNN_WARPS * 32)
-k_dens_gather(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
-              const int* __restrict__ idx33, const float* __restrict__ rk,
-              float4* __restrict__ vel)
+k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
+               const int* __restrict__ idx33, const float* __restrict__ rk,
+               const int* __restrict__ dexp, unsigned long long* __restrict__ acc)
 {
     __shared__ int stk[KNN_WARPS][STACK_MAX];
-    __shared__ float4 cpos[KNN_WARPS][32];
-    __shared__ float4 cpar[KNN_WARPS][32];  // t33, idx33 bits, hinv, -
+    __shared__ float4 cand[KNN_WARPS][32];
+    __shared__ float cscale[KNN_WARPS][32];  // 2^(FIX_BITS - e_j)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = t.n;
     const int base = (blockIdx.x * KNN_WARPS + warp) * 32;
     if (base >= n) return;
-    const int j = min(base + lane, n - 1);
-    const float4 xj = pos[j];
-    const int idx_j = __float_as_int(xj.w);
-    float hi = 0.0f, lo = 0.0f;
-
-    auto inside = [&](float4 l, float4 h) {
-        return xj.x >= l.x && xj.x <= h.x && xj.y >= l.y && xj.y <= h.y && xj.z >= l.z &&
-               xj.z <= h.z;
-    };
-    auto child_in = [&](int c) {
-        if (c < 0) {
-            const float4 p = pos[~c];
-            const float h = __fmul_ru(rk[~c], 1.000001f);
-            return inside(make_float4(__fsub_rd(p.x, h), __fsub_rd(p.y, h), __fsub_rd(p.z, h), 0.f),
-                          make_float4(__fadd_ru(p.x, h), __fadd_ru(p.y, h), __fadd_ru(p.z, h), 0.f));
-        }
-        return inside(t.elo[c], t.ehi[c]);
-    };
+    const bool valid = base + lane < n;
+    const int q = min(base + lane, n - 1);
+    const float4 xq = pos[q];
+    const float T = valid ? t33[q] : -1.0f;  // a padding lane takes nothing
+    const int i33 = idx33[q];
+    const float hinv = __fdiv_rn(1.0f, rk[q]);
 
     int* st = stk[warp];
     if (lane == 0) st[0] = tree_root(n);
@@ -278,8 +292,8 @@ k_dens_gather(const float4* __restrict__ pos, TreeView t, const float* __restric
         } else {
             const int4 m = t.meta[node];
             if (m.w - m.z + 1 > t.leaf) {
-                const bool v0 = __any_sync(FULL, child_in(m.x));
-                const bool v1 = __any_sync(FULL, child_in(m.y));
+                const bool v0 = __any_sync(FULL, child_dist2(pos, t, m.x, xq) <= T);
+                const bool v1 = __any_sync(FULL, child_dist2(pos, t, m.y, xq) <= T);
                 if (sp + 2 > STACK_MAX) break;  // k_knn_t33 already flagged the same tree
                 if (lane == 0) {
                     if (v1) st[sp] = m.y;
@@ -294,30 +308,38 @@ k_dens_gather(const float4* __restrict__ pos, TreeView t, const float* __restric
         }
         const int cnt = last - first + 1;
         if (lane < cnt) {
-            const int s = first + lane;
-            cpos[warp][lane] = pos[s];
-            cpar[warp][lane] = make_float4(t33[s], __int_as_float(idx33[s]),
-                                           __fdiv_rn(1.0f, rk[s]), 0.0f);
+            cand[warp][lane] = pos[first + lane];
+            cscale[warp][lane] = __int_as_float((127 + FIX_BITS - dexp[first + lane]) << 23);
         }
         __syncwarp();
         for (int k = 0; k < cnt; ++k) {
-            const float4 c = cpos[warp][k];
-            const float4 pr = cpar[warp][k];
-            const float d2 = norm2_rn(c.x, c.y, c.z, xj.x, xj.y, xj.z);
-            const bool member = d2 < pr.x || (d2 == pr.x && idx_j < __float_as_int(pr.y));
+            const float4 c = cand[warp][k];
+            const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
+            const bool member = d2 < T || (d2 == T && __float_as_int(c.w) < i33);
             if (__any_sync(FULL, member)) {
-                const float w = member ? ker_rn(c.x, c.y, c.z, xj.x, xj.y, xj.z, pr.z) : 0.0f;
-                two_sum_acc(hi, lo, w);
+                const float w = member ? ker_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z, hinv) : 0.0f;
+                const unsigned long long f = __float2ull_rn(__fmul_rn(w, cscale[warp][k]));
+                const unsigned s0 = __reduce_add_sync(FULL, (unsigned)(f & 0x3fffffull));
+                const unsigned s1 = __reduce_add_sync(FULL, (unsigned)(f >> 22));
+                if (lane == 0)
+                    atomicAdd(&acc[first + k], (unsigned long long)s0 + ((unsigned long long)s1 << 22));
             }
         }
         __syncwarp();
     }
-    // dens accumulates onto the incoming value, as q->dens += ... does
-    if (base + lane < n) {
-        float4 v = vel[base + lane];
-        v.w = __fadd_rn(v.w, __fadd_rn(hi, lo));
-        vel[base + lane] = v;
-    }
+}
+
+// dens_j += acc_j * 2^(e_j - FIX_BITS), one rounding to float
+__global__ void k_dens_finish(const unsigned long long* __restrict__ acc,
+                              const int* __restrict__ dexp, int n, float4* __restrict__ vel)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double scale = __longlong_as_double((long long)(1023 + dexp[j] - FIX_BITS) << 52);
+    const float d = __double2float_rn(__dmul_rn(__ull2double_rn(acc[j]), scale));
+    float4 v = vel[j];
+    v.w = __fadd_rn(v.w, d);  // dens accumulates onto the incoming value, as q->dens += ... does
+    vel[j] = v;
 }
 
 static int knn_blocks(int n) { return (n + KNN_WARPS * 32 - 1) / (KNN_WARPS * 32); }
@@ -338,12 +360,15 @@ void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int
     count_launches(1);
 }
 
-void launch_dens_gather(const float4* pos, const TreeView& t, const float* t33,
-                        const int* idx33, const float* rk, float4* vel, cudaStream_t s)
+void launch_dens(const float4* pos, const TreeView& t, const float* t33, const int* idx33,
+                 const float* rk, int* dexp, unsigned long long* acc, float4* vel, cudaStream_t s)
 {
     if (t.n <= 0) return;
-    k_dens_gather<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, rk, vel);
-    count_launches(1);
+    const int nb = (t.n + 255) / 256;
+    k_dens_prep<<<nb, 256, 0, s>>>(rk, t.n, dexp, acc);
+    k_dens_scatter<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, rk, dexp, acc);
+    k_dens_finish<<<nb, 256, 0, s>>>(acc, dexp, t.n, vel);
+    count_launches(3);
 }
 
 }  // namespace asg

@@ -35,7 +35,7 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 struct NoallocLayout {
     size_t pos_in, vel_in, igrp_in, rk_in, keys0, keys1, vals0, vals1, sort_tmp;
     size_t pos, vel, igrp, rk, t33, idx33, meta, parent, leaf_parent, flags;
-    size_t blo, bhi, elo, ehi, err, total;
+    size_t blo, bhi, dacc, dexp, err, total;
 };
 
 static constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -71,8 +71,8 @@ static NoallocLayout noalloc_layout(size_t n)
     L.flags = take(4 * m);
     L.blo = take(16 * m);
     L.bhi = take(16 * m);
-    L.elo = take(16 * m);
-    L.ehi = take(16 * m);
+    L.dacc = take(8 * n);
+    L.dexp = take(4 * n);
     L.err = take(16);
     L.total = o;
     return L;
@@ -171,22 +171,19 @@ extern "C" int asg_neighbor_search_noalloc(const float* d_x, int np, float left,
                          F4(L.vel), I(L.igrp), F(L.rk), s);
     launch_build_tree(keys, np, reinterpret_cast<int4*>(b + L.meta), I(L.parent), I(L.leaf_parent),
                       s);
-    launch_tree_boxes(F4(L.pos), nullptr, np, reinterpret_cast<int4*>(b + L.meta), I(L.parent),
-                      I(L.leaf_parent), I(L.flags), F4(L.blo), F4(L.bhi), s);
+    launch_tree_boxes(F4(L.pos), nullptr, np, LEAF_MAX, reinterpret_cast<int4*>(b + L.meta),
+                      I(L.parent), I(L.flags), F4(L.blo), F4(L.bhi), s);
     TreeView t;
     t.n = np;
     t.leaf = LEAF_MAX;
     t.meta = reinterpret_cast<const int4*>(b + L.meta);
     t.blo = F4(L.blo);
     t.bhi = F4(L.bhi);
-    t.elo = F4(L.elo);
-    t.ehi = F4(L.ehi);
     launch_knn_t33(F4(L.pos), t, F(L.t33), F(L.rk), I(L.idx33), err, s);
     launch_knn_ties(F4(L.pos), t, F(L.t33), I(L.idx33), 0, err, s);
     launch_check_rk(F(L.rk), np, err, s);
-    launch_tree_boxes(F4(L.pos), F(L.rk), np, reinterpret_cast<int4*>(b + L.meta), I(L.parent),
-                      I(L.leaf_parent), I(L.flags), F4(L.elo), F4(L.ehi), s);
-    launch_dens_gather(F4(L.pos), t, F(L.t33), I(L.idx33), F(L.rk), F4(L.vel), s);
+    launch_dens(F4(L.pos), t, F(L.t33), I(L.idx33), F(L.rk), I(L.dexp),
+                reinterpret_cast<unsigned long long*>(b + L.dacc), F4(L.vel), s);
     k_noalloc_store<<<(np + 255) / 256, 256, 0, s>>>(perm, F(L.rk), F4(L.vel), np, d_rk, d_dens);
     count_launches(1);
 

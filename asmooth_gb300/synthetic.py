@@ -278,6 +278,29 @@ WORKLOADS = {
 }
 
 
+def make_batch(seed: int = 4, scale: int = 1, n_cubes: int = 27,
+               contractions=(1.0, 0.7, 0.5)) -> tuple[list, tuple]:
+    """The batched workload: ``n_cubes`` node-cubes of side 256 (mean
+    separation 2, so 128^3 particles on average), each with its own halo
+    fraction f ~ U[0.2, 0.8] and a particle count 128^3 * (1 + (f - 0.5)/2)
+    that varies with it, NFW halos as in the 256^3 cube (625 per cube), and
+    one item per redshift with every halo contracted by the given factor about
+    its centre.  Items are ordered cube-major; nc = 32, 64, 128."""
+    rng = np.random.default_rng(seed)
+    box = 256.0 / scale
+    npd = 128 // scale
+    items = []
+    for c in range(n_cubes):
+        f = float(rng.uniform(0.2, 0.8))
+        n = int(round(npd ** 3 * (1.0 + 0.5 * (f - 0.5))))
+        for con in contractions:
+            x, v = nfw_cube(n, box, 1000 * seed + c, frac_halo=f, n_halos=max(8, 625 // scale ** 3),
+                            halo_contraction=con)
+            items.append(add_periodic_shell(x, v, box, 8.0))
+    ncs = tuple(max(4, nc // scale) for nc in (32, 64, 128))
+    return items, ncs
+
+
 def make_workload(name: str, seed: int | None = None, scale: int = 1) -> tuple[Cube, tuple]:
     """Build a named workload with its 8-unit periodic shell.  ``scale`` > 1
     divides the particle count per dimension and the box side by ``scale`` (same

@@ -32,6 +32,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particles/s, k=32 kNN + SPH deposit at 256^3: mixed vs plain FP32 on 1 GB300"
 WORKLOAD = "cfg2"  # 256^3 particles, side 512, 5000 NFW halos, nc = 64,128,256
+# --workload choices: (generator name, scale divisor, description)
+WORKLOADS = {
+    "cfg2": ("cfg2", 1, "cfg2: 256^3 particles, side 512, 5000 NFW halos, 8-unit periodic shell, "
+                        "k=32, nc=64,128,256"),
+    "cfg2_s2": ("cfg2", 2, "cfg2 model at 1/8 volume: 128^3 particles, side 256, 625 NFW halos, "
+                           "8-unit periodic shell, k=32, nc=32,64,128"),
+    "cfg5": ("cfg5", 1, "cfg5: 512^3 particles, side 1024, 20000 NFW halos, 8-unit periodic "
+                        "shell, k=32, nc=128,256,512"),
+}
 CPU_SAMPLE = ("cfg2", 2)  # same model at 1/8 volume: 128^3 particles, side 256, nc = 32,64,128
 
 
@@ -215,8 +224,8 @@ def run_ours(args):
     from asmooth_gb300 import synthetic as syn
 
     seed = 2 + 1000 * rank  # independent replica cube per rank
-    scale = 2 if args.workload == "cfg2_s2" else 1
-    cube, ncs = syn.make_workload(WORKLOAD, seed=seed, scale=scale)
+    gen, scale, wl_desc = WORKLOADS[args.workload]
+    cube, ncs = syn.make_workload(gen, seed=seed, scale=scale)
     n, n_local = cube.n, cube.n_local
     x_d = torch.from_numpy(cube.x).cuda()
     v_d = torch.from_numpy(cube.v).cuda()
@@ -329,6 +338,23 @@ def run_ours(args):
             "step_hbm_gbs_vs_peak": {"achieved": hbm_alg / (ms_step * 1e-3) / 1e9,
                                      "peak": pk["hbm_gbs"], "peak_kind": pk_kind}}
 
+    # friends-of-friends beside the path (linking length 0.2 x mean separation 2)
+    fof = None
+    if args.fof:
+        ctx.load_particles_device(x_d.data_ptr(), n, cube.left, cube.right, v_ptr=v_d.data_ptr())
+        ng = ctx.run_fof(0.4)
+        ms_f = []
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ng = ctx.run_fof(0.4)
+            e1.record(stream)
+            e1.synchronize()
+            ms_f.append(e0.elapsed_time(e1))
+        fof = {"ll": 0.4, "groups": ng, "ms": statistics.median(ms_f),
+               "particles_per_s": n / (statistics.median(ms_f) * 1e-3)}
+
     # mixed-precision form: positions as int32 cell index + uint16 offsets in
     # 4-unit cells, decoded on the device, then the same FP32 path
     mixed = None
@@ -384,6 +410,30 @@ def run_ours(args):
                             "d2h_bytes_per_step": 8 * n + sum(4 * 6 * nc ** 3 for nc in ncs)
                             + 16 * len(ncs)}
 
+    # batched form: the 27-cube x 3-redshift workload through one CUDA graph
+    batch = None
+    if args.batch:
+        items, bncs = syn.make_batch(scale=args.batch_scale)
+        with api.Batch(ctx, items, bncs) as bt:
+            tuned = bt.tune() if args.tune else None
+            bt.run()  # plan, capture, first replay
+            gms = []
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                bt.run()
+                gms.append(bt.stats()["graph_ms"])
+            st = bt.stats()
+        g = max_over_ranks(statistics.median(gms), dist)
+        batch = {"items": len(items), "nc": list(bncs), "particles_local": st["particles_local"],
+                 "particles_with_shell": int(sum(c.n for c in items)),
+                 "graph_ms": g, "value": replica_value(st["particles_local"], world, g * 1e-3),
+                 "unit": "particles/s", "kernels_per_graph": st["kernels"],
+                 "tuned_leaf_seg": tuned,
+                 "workload": "27 cubes of side 256 (128^3 +- clustering-dependent count, halo "
+                             "fraction U[0.2,0.8]) x 3 redshifts (halos contracted 1, 0.7, 0.5)"
+                             + (f", scale 1/{args.batch_scale}" if args.batch_scale > 1 else "")}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -400,8 +450,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded NFW-clustered cube in cubep3m layout)",
-        "config": {"workload": "cfg2: 256^3 particles, side 512, 5000 NFW halos, 8-unit periodic "
-                               "shell, k=32, nc=64,128,256, plain FP32 form",
+        "config": {"workload": wl_desc + ", plain FP32 form",
                    "n_with_shell": n, "n_local": n_local, "parallelism": f"replicas x{world}",
                    "l2": "flushed before every timed step; inputs larger than L2"},
         "e2e": e2e,
@@ -412,6 +461,10 @@ def run_ours(args):
     }
     if mixed:
         line["mixed"] = mixed
+    if fof:
+        line["fof"] = fof
+    if batch:
+        line["batch"] = batch
     if cpu:
         line["cpu_baseline"] = cpu
     if rank == 0:
@@ -431,8 +484,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg2_s2"],
-                    help="cfg2_s2: the same model at 1/8 volume, for profiling captures")
+    ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS),
+                    help="cfg2_s2: the cfg2 model at 1/8 volume, for profiling captures; "
+                         "cfg5: the 512^3 cube")
+    ap.add_argument("--fof", action="store_true",
+                    help="also time GPU FOF (linking length 0.4) on the loaded cube")
+    ap.add_argument("--batch", action="store_true",
+                    help="also time the batched form (27 cubes x 3 redshifts, one CUDA graph)")
+    ap.add_argument("--batch-scale", type=int, default=1,
+                    help="divide the batched cubes' side by this (quick runs)")
+    ap.add_argument("--tune", action="store_true", help="autotune the batched form first")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -265,6 +265,39 @@ int asg_smooth_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off, con
                          const int* ncs, int n_nc, int sign, float* rk, float* dens,
                          float* const* meshes, double* totals);
 
+/* ---- batched form ---------------------------------------------------------------
+ * No counterpart in the reference, which runs one node-cube per MPI rank and
+ * redshift: many cubes (or one cube at several redshifts) of uneven particle
+ * counts run through the whole path in one CUDA graph.  Item i has np[i]
+ * particles (with its shell) in [left[i], right[i]), box side boxsize[i];
+ * every item gets the meshes ncs[0..n_nc-1] with the given sign.  The batch
+ * owns device input and output arrays for all items.  The first
+ * asg_batch_run plans (one eager pass that sizes every buffer and records
+ * each item's pair count) and captures the per-item kernels into one graph;
+ * later runs replay it.  Inputs whose pair counts outgrow the plan by more
+ * than 1/16 are re-planned automatically.  Results equal asg_smooth's on each
+ * item.  A batch uses its context exclusively until it is destroyed. */
+typedef struct asg_batch asg_batch;
+int asg_batch_create(asg_ctx* ctx, int n_items, const int* np, const int* np_local,
+                     const float* left, const float* right, const float* boxsize, const int* ncs,
+                     int n_nc, int sign, asg_batch** batch);
+void asg_batch_destroy(asg_batch* batch);
+/* Item positions x (np*3) and velocities v (np*3, may be NULL = 0), host or
+ * device pointers. */
+int asg_batch_set_item(asg_batch* batch, int item, const float* x, const float* v, int device_ptrs);
+/* Optional autotuner: times the largest item with tree bucket sizes 16, 24, 32
+ * and deposit work items of 2048, 4096, 8192 pairs and keeps the fastest. */
+int asg_batch_tune(asg_batch* batch, int* leaf, int* seg);
+int asg_batch_run(asg_batch* batch);
+/* Device time of the last graph launch (ms), kernels per launch, and the
+ * interior particles of all items (the numerator of the batched metric). */
+int asg_batch_stats(asg_batch* batch, double* graph_ms, long long* kernels,
+                    long long* particles_local);
+/* Results of one item: rk, dens (np each, input order), meshes[k] (6*nc^3),
+ * totals (2 per mesh); any may be NULL. */
+int asg_batch_get(asg_batch* batch, int item, float* rk, float* dens, float* const* meshes,
+                  double* totals);
+
 /* CUDA stream used by the context (cudaStream_t as void*). */
 void* asg_stream(asg_ctx* ctx);
 /* Count of kernels this library has launched so far (process-wide). */
@@ -275,7 +308,7 @@ long long asg_kernel_launches(asg_ctx* ctx);
  * and zeroes the accumulators; asg_phase_ms fills ms[0..ASG_NPHASES-1] with the
  * device time accumulated per phase since then. */
 #define ASG_NPHASES 8
-enum { ASG_PH_INDEX = 0, ASG_PH_KNN = 1, ASG_PH_TIES = 2, ASG_PH_BOXES = 3, ASG_PH_DENS = 4,
+enum { ASG_PH_INDEX = 0, ASG_PH_KNN = 1, ASG_PH_TIES = 2, ASG_PH_CHECK = 3, ASG_PH_DENS = 4,
        ASG_PH_DEPOSIT = 5, ASG_PH_HALOS = 6, ASG_PH_FOF = 7 };
 int asg_set_timing(asg_ctx* ctx, int enable);
 int asg_phase_ms(asg_ctx* ctx, double* ms);

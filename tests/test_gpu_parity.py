@@ -269,6 +269,27 @@ def test_lattice_ties_by_index(gpu_ctx, oracle):
     assert np.max(np.abs(p["dens"] - d64) / d64) <= FIELD_TOL
 
 
+@pytest.mark.parametrize("leaf", ["1", "7"])
+def test_other_bucket_sizes(oracle, leaf, monkeypatch):
+    """Tree buckets of 1 and 7 particles (ASG_LEAF_SIZE): the same exact
+    neighbours, FOF groups and halo marks (the node boxes are built for the
+    bucket size in use)."""
+    monkeypatch.setenv("ASG_LEAF_SIZE", leaf)
+    cube, _ = syn.make_workload("cfg1", scale=4)
+    x = cube.x
+    with api.Context(0) as ctx:
+        p = api.make_particles(x, cube.v)
+        ctx.neighbor_search(p, cube.left, cube.right)
+        t33, idx33 = ctx.get_knn(cube.n)
+        te, ie, _ = oracle.knn_exact(x, cube.left, cube.right, NTHREADS)
+        assert np.array_equal(bits(t33), bits(te)) and np.array_equal(idx33, ie)
+        q = api.make_particles(x)
+        ng = ctx.group_fof(q, cube.left, cube.right, np.float32(0.4))
+        lab, ng_ref = oracle.group_fof(x, cube.left, cube.right, np.float32(0.4), exact=True)
+        assert ng == ng_ref
+        assert np.array_equal(po.canonical_groups(q["igrp"]), po.canonical_groups(lab))
+
+
 def test_empty_halo_list_and_small_sets(gpu_ctx):
     x = np.random.default_rng(9).uniform(0, 10, (33, 3)).astype(np.float32)
     p = api.make_particles(x)
