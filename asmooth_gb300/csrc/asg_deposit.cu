@@ -462,28 +462,7 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                 const float rx = c_rcp[nx], rxy = c_rcp[nxy];
                 const float* wp = S.w[p];
                 const bool hal = (rp >> 24) != 0;
-                // column mapping when it needs no more passes than the packed one
-                const int lpi = nxy <= 32 ? small_div(32, rxy) : 0;
-                const bool columns =
-                    lpi > 0 && small_div(nz + lpi - 1, c_rcp[lpi]) <= ((ncell + 31) >> 5);
-                if (columns) {
-                    // each lane owns one (x, y) column and steps through z: lpi
-                    // layers of nx*ny lanes per pass; (wx*wy) once per pair
-                    const int lz = small_div(lane, rxy);
-                    const int r = lane - lz * nxy;
-                    const int ly = small_div(r, rx);
-                    const int gx = x0 + r - ly * nx, gy = y0 + ly;
-                    if (lz < lpi) {
-                        const float wxy = __fmul_rn(wp[gx], wp[TS + gy]);
-                        const int sb = gy << 3, xr = gx + 6 * gy;
-                        for (int gz = z0 + lz; gz < z0 + nz; gz += lpi) {
-                            const float w3 = __fmul_rn(wxy, wp[2 * TS + gz]);
-                            const int slot = (gz << 6) | sb | ((xr + 4 * gz) & (TS - 1));
-                            if (!hal) add_cell(S, slot, w3, dens, vx, vy, vz);
-                            else add_halo(S, slot, w3);
-                        }
-                    }
-                } else if (!hal) {
+                if (!hal) {
                     for (int c = lane; c < ncell; c += 32) {
                         const int iz = small_div(c, rxy);
                         const int rem = c - iz * nxy;

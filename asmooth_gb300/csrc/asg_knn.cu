@@ -278,6 +278,7 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
     const float T = valid ? t33[q] : -1.0f;  // a padding lane takes nothing
     const int i33 = idx33[q];
     const float hinv = __fdiv_rn(1.0f, rk[q]);
+    const bool any_tie = __any_sync(FULL, valid && i33 >= 0);  // warp-uniform
 
     int* st = stk[warp];
     if (lane == 0) st[0] = tree_root(n);
@@ -315,7 +316,8 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
         for (int k = 0; k < cnt; ++k) {
             const float4 c = cand[warp][k];
             const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
-            const bool member = d2 < T || (d2 == T && __float_as_int(c.w) < i33);
+            // the index rule matters only where the 33rd distance is tied
+            const bool member = d2 < T || (any_tie && d2 == T && __float_as_int(c.w) < i33);
             if (__any_sync(FULL, member)) {
                 const float w = member ? ker_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z, hinv) : 0.0f;
                 const unsigned long long f = __float2ull_rn(__fmul_rn(w, cscale[warp][k]));

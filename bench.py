@@ -320,15 +320,18 @@ def run_ours(args):
     achieved = alg[dom] / (per_step[dom] * 1e-3) / 1e12
     # DRAM bytes of one launch of the dominant kernel: the per-particle figure of
     # an ncu capture of a smaller cube, times this launch's particles
-    traffic = None
+    traffic, pipes = None, None
     tpath = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
     if os.path.exists(tpath):
         rec = json.load(open(tpath)).get(dom)
         if rec:
             traffic = rec["bytes_per_particle"] * n
+            # what bounds the kernel instead of FMA throughput: ALU pipe and issue slots
+            pipes = {k: rec[k] for k in ("alu_pipe_pct_of_peak", "fma_pipe_pct_of_peak",
+                                         "issue_active_pct", "kernel", "capture") if k in rec}
     hbm_alg = n * (12 + 8 + 36) + sum(24 * nc ** 3 for nc in ncs)
     roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": fp32, "unit": "TFLOP/s",
-            "frac": achieved / fp32, "traffic": traffic,
+            "frac": achieved / fp32, "traffic": traffic, "pipe_utilisation_ncu": pipes,
             "peak_source": "measured FMA-chain kernel on this GPU (no FP32 figure in the peaks file)",
             "phase_ms_per_step": per_step,
             "alg_flops_per_step": alg,
