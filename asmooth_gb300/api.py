@@ -468,6 +468,9 @@ class Batch:
             raise ValueError("item size is fixed at creation")
         self.ctx._ok(self.lib.asg_batch_set_item(self.h, int(i), _ptr(x), _ptr(v), 0))
 
+    def set_streams(self, streams: int):
+        self.ctx._ok(self.lib.asg_batch_set_streams(self.h, int(streams)))
+
     def tune(self):
         leaf, seg = C.c_int(0), C.c_int(0)
         self.ctx._ok(self.lib.asg_batch_tune(self.h, C.byref(leaf), C.byref(seg)))

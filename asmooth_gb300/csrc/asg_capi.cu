@@ -1480,6 +1480,10 @@ struct asg_batch {
     long long launches = 0;        // kernels per graph launch
     double last_ms = 0.0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // concurrent streams: item i runs on sub[i % sub.size()]; sub[0] is ctx, the
+    // others are contexts of the batch (own stream and scratch) joined in the graph
+    std::vector<asg_ctx*> sub;
+    std::vector<cudaEvent_t> fork, join;
 };
 
 namespace {
@@ -1492,11 +1496,11 @@ void batch_drop_graph(asg_batch* b)
     b->graph = nullptr;
 }
 
-// one item's whole path on the context stream; cap = 0 sizes the deposit from
-// its pair count (one synchronisation), cap > 0 synchronises nowhere
-int batch_queue_item(asg_batch* b, int i, uint32_t cap)
+// one item's whole path on the stream of ctx (the batch's context or one of its
+// sub-contexts); cap = 0 sizes the deposit from its pair count (one
+// synchronisation), cap > 0 synchronises nowhere
+int batch_queue_item(asg_batch* b, asg_ctx* ctx, int i, uint32_t cap)
 {
-    asg_ctx* ctx = b->ctx;
     const int n = b->np[(size_t)i];
     const size_t o = b->off[(size_t)i];
     ctx->n = n;
@@ -1530,41 +1534,67 @@ int batch_queue_item(asg_batch* b, int i, uint32_t cap)
 int batch_plan(asg_batch* b)
 {
     asg_ctx* ctx = b->ctx;
-    if (int r = alloc_set(ctx, b->max_n)) return r;
-    if (int r = grow(ctx, ctx->lab_scan, 4 * (size_t)b->max_n)) return r;
+    const size_t S = b->sub.size();
+    for (asg_ctx* c : b->sub) {
+        c->leaf = ctx->leaf;  // the tuned configuration applies to every stream
+        c->dep_seg = ctx->dep_seg;
+        if (int r = alloc_set(c, b->max_n)) return fail(ctx, r, "batch: stream scratch");
+        if (int r = grow(c, c->lab_scan, 4 * (size_t)b->max_n)) return fail(ctx, r, "batch: stream scratch");
+    }
     b->cap.assign((size_t)b->n_items, 0u);
     uint32_t max_cap = 0;
     for (int i = 0; i < b->n_items; ++i) {
-        if (int r = batch_queue_item(b, i, 0)) return r;
-        const uint32_t np = ctx->dep_npairs;
+        asg_ctx* c = b->sub[(size_t)i % S];
+        if (int r = batch_queue_item(b, c, i, 0)) return fail(ctx, r, c->last);
+        const uint32_t np = c->dep_npairs;
         b->cap[(size_t)i] = np + np / 16 + 4096;  // headroom for inputs that change between runs
         max_cap = std::max(max_cap, b->cap[(size_t)i]);
     }
-    if (int r = finish(ctx, "batch plan")) return r;
+    for (asg_ctx* c : b->sub)
+        if (int r = finish(c, "batch plan")) return fail(ctx, r, c->last);
     // reserve the deposit arrays for the largest capacity, so that the capture allocates nothing
     const size_t NP = (size_t)max_cap + 1;
-    if (int r = grow(ctx, ctx->dep_pairs, 16 * NP)) return r;
-    if (int r = grow(ctx, ctx->dep_sort, radix_sort_temp_bytes((int)NP))) return r;
-    const uint32_t items = deposit_max_items(ctx->dep_tiles_n, max_cap, ctx->dep_seg);
-    return grow(ctx, ctx->dep_partial, deposit_partial_bytes(items) + 16);
+    for (asg_ctx* c : b->sub) {
+        int r = grow(c, c->dep_pairs, 16 * NP);
+        if (!r) r = grow(c, c->dep_sort, radix_sort_temp_bytes((int)NP));
+        const uint32_t items = deposit_max_items(c->dep_tiles_n, max_cap, c->dep_seg);
+        if (!r) r = grow(c, c->dep_partial, deposit_partial_bytes(items) + 16);
+        if (r) return fail(ctx, r, "batch: deposit reserve");
+    }
+    return 0;
 }
 
 int batch_capture(asg_batch* b)
 {
     asg_ctx* ctx = b->ctx;
     batch_drop_graph(b);
-    const bool timing = ctx->timing;
-    ctx->timing = false;
+    const size_t S = b->sub.size();
+    std::vector<bool> timing;
+    for (asg_ctx* c : b->sub) {
+        timing.push_back(c->timing);
+        c->timing = false;
+    }
     const long long l0 = g_launches.load();
     cudaError_t e = cudaStreamBeginCapture(ctx->s, cudaStreamCaptureModeThreadLocal);
     int r = e == cudaSuccess ? 0 : cuda_fail(ctx, e, "cudaStreamBeginCapture");
-    for (int i = 0; !r && i < b->n_items; ++i) r = batch_queue_item(b, i, b->cap[(size_t)i]);
+    if (!r && S > 1) {  // fork: every stream starts after the capture origin
+        if (cudaEventRecord(b->fork[0], ctx->s) != cudaSuccess) r = fail(ctx, ASG_ERR_CUDA, "fork");
+        for (size_t s = 1; !r && s < S; ++s)
+            if (cudaStreamWaitEvent(b->sub[s]->s, b->fork[0], 0) != cudaSuccess)
+                r = fail(ctx, ASG_ERR_CUDA, "fork");
+    }
+    for (int i = 0; !r && i < b->n_items; ++i)
+        r = batch_queue_item(b, b->sub[(size_t)i % S], i, b->cap[(size_t)i]);
+    for (size_t s = 1; !r && s < S; ++s)  // join: the origin stream waits for every stream
+        if (cudaEventRecord(b->join[s], b->sub[s]->s) != cudaSuccess ||
+            cudaStreamWaitEvent(ctx->s, b->join[s], 0) != cudaSuccess)
+            r = fail(ctx, ASG_ERR_CUDA, "join");
     cudaGraph_t g = nullptr;
     if (e == cudaSuccess) {
         const cudaError_t e2 = cudaStreamEndCapture(ctx->s, &g);
         if (!r && e2 != cudaSuccess) r = cuda_fail(ctx, e2, "cudaStreamEndCapture");
     }
-    ctx->timing = timing;
+    for (size_t s = 0; s < S; ++s) b->sub[s]->timing = timing[s];
     b->launches = g_launches.load() - l0;
     if (r) {
         if (g) cudaGraphDestroy(g);
@@ -1629,6 +1659,11 @@ int asg_batch_create(asg_ctx* ctx, int n_items, const int* np, const int* np_loc
     if (!r) r = grow(ctx, b->out_tot, 16 * (size_t)n_items * n_nc);
     if (!r && (cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess))
         r = fail(ctx, ASG_ERR_CUDA, "cudaEventCreate");
+    b->sub.push_back(ctx);
+    b->fork.assign(1, nullptr);
+    b->join.assign(1, nullptr);
+    if (!r && cudaEventCreateWithFlags(&b->fork[0], cudaEventDisableTiming) != cudaSuccess)
+        r = fail(ctx, ASG_ERR_CUDA, "cudaEventCreate");
     if (!r) r = cudaMemsetAsync(b->in_v.p, 0, 12 * b->n_total, ctx->s) == cudaSuccess
                     ? 0 : fail(ctx, ASG_ERR_CUDA, "memset");
     if (r) {
@@ -1649,7 +1684,38 @@ void asg_batch_destroy(asg_batch* b)
         if (x->p) cudaFree(x->p);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
+    for (size_t s = 1; s < b->sub.size(); ++s) asg_destroy(b->sub[s]);
+    for (cudaEvent_t e : b->fork)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : b->join)
+        if (e) cudaEventDestroy(e);
     delete b;
+}
+
+int asg_batch_set_streams(asg_batch* b, int streams)
+{
+    if (!b || streams < 1 || streams > 8) return ASG_ERR_ARG;
+    asg_ctx* ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device));
+    batch_drop_graph(b);
+    while ((int)b->sub.size() > streams) {
+        asg_destroy(b->sub.back());
+        b->sub.pop_back();
+        if (b->join.back()) cudaEventDestroy(b->join.back());
+        b->join.pop_back();
+    }
+    while ((int)b->sub.size() < streams) {
+        asg_ctx* c = nullptr;
+        if (int r = asg_create(&c, ctx->device)) return fail(ctx, r, "batch: stream context");
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            asg_destroy(c);
+            return fail(ctx, ASG_ERR_CUDA, "cudaEventCreate");
+        }
+        b->sub.push_back(c);
+        b->join.push_back(e);
+    }
+    return ASG_OK;
 }
 
 int asg_batch_set_item(asg_batch* b, int item, const float* x, const float* v, int device_ptrs)
@@ -1685,7 +1751,7 @@ int asg_batch_tune(asg_batch* b, int* leaf, int* seg)
             float ms = 0.0f;
             for (int rep = 0; rep < 2; ++rep) {  // the first repetition warms up
                 CK(cudaEventRecord(b->e0, ctx->s));
-                if (int r = batch_queue_item(b, item, 0)) return r;
+                if (int r = batch_queue_item(b, ctx, item, 0)) return r;
                 CK(cudaEventRecord(b->e1, ctx->s));
                 CK(cudaEventSynchronize(b->e1));
                 CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
@@ -1718,7 +1784,11 @@ int asg_batch_run(asg_batch* b)
         CK(cudaGraphLaunch(b->exec, ctx->s));
         CK(cudaEventRecord(b->e1, ctx->s));
         count_launches((int)b->launches);
-        const int r = finish(ctx, "batch run");
+        int r = finish(ctx, "batch run");
+        for (size_t s = 1; s < b->sub.size(); ++s) {  // the other streams' error words
+            const int rs = finish(b->sub[s], "batch run");
+            if (rs && (!r || r == ASG_ERR_STATE)) r = fail(ctx, rs, b->sub[s]->last);
+        }
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, b->e0, b->e1) == cudaSuccess) b->last_ms = ms;
         if (r != ASG_ERR_STATE) return r;  // ERR_CAP: the inputs outgrew the plan

@@ -26,12 +26,14 @@
 //      segment order.
 // n, c and halo are double-float (two-sum) sums, so the per-tile FP64 totals
 // reproduce the FP64 sum of the float weights.
+#include <atomic>
+
 #include "asg_common.cuh"
 #include "asg_internal.h"
 
 namespace asg {
 
-constexpr int TS = 8;              // tile edge in cells
+constexpr int TS = 8;             // tile edge in cells
 constexpr int TC = TS * TS * TS;   // cells per tile
 constexpr int DEP_THREADS = 256;   // threads of the tile-merge CTA
 constexpr int SEG_DEFAULT = 4096;  // pairs per work item unless DepositParams::seg says otherwise
@@ -620,14 +622,15 @@ void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t
     exclusive_scan_u32(w.item_off, (size_t)T + 1, w.scan_tmp_t, s);
     cudaMemsetAsync(w.next_item, 0, sizeof(int), s);
     const size_t smem = DEP_WARPS * sizeof(WarpTile);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_deposit_items, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_deposit_items, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        attr = true;
-    }
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
+    static std::atomic<unsigned long long> attr_set{0};  // one bit per device (function attributes are per device)
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_set.load() & bit)) {
+        cudaFuncSetAttribute(k_deposit_items, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_deposit_items, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        attr_set.fetch_or(bit);
+    }
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_items, 32 * DEP_WARPS, smem);
     const int grid = sms * (per_sm > 0 ? per_sm : 1);

@@ -419,6 +419,7 @@ def run_ours(args):
         items, bncs = syn.make_batch(scale=args.batch_scale)
         with api.Batch(ctx, items, bncs) as bt:
             tuned = bt.tune() if args.tune else None
+            bt.set_streams(args.batch_streams)
             bt.run()  # plan, capture, first replay
             gms = []
             for _ in range(args.steps):
@@ -432,7 +433,7 @@ def run_ours(args):
                  "particles_with_shell": int(sum(c.n for c in items)),
                  "graph_ms": g, "value": replica_value(st["particles_local"], world, g * 1e-3),
                  "unit": "particles/s", "kernels_per_graph": st["kernels"],
-                 "tuned_leaf_seg": tuned,
+                 "tuned_leaf_seg": tuned, "streams": args.batch_streams,
                  "workload": "27 cubes of side 256 (128^3 +- clustering-dependent count, halo "
                              "fraction U[0.2,0.8]) x 3 redshifts (halos contracted 1, 0.7, 0.5)"
                              + (f", scale 1/{args.batch_scale}" if args.batch_scale > 1 else "")}
@@ -497,6 +498,8 @@ def main():
     ap.add_argument("--batch-scale", type=int, default=1,
                     help="divide the batched cubes' side by this (quick runs)")
     ap.add_argument("--tune", action="store_true", help="autotune the batched form first")
+    ap.add_argument("--batch-streams", type=int, default=4,
+                    help="concurrent streams inside the batched form's graph")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

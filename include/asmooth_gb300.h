@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define ASG_ABI_VERSION 1
+#define ASG_ABI_VERSION 2
 
 typedef struct asg_particle {
     float x[3], v[3];
@@ -285,6 +285,10 @@ void asg_batch_destroy(asg_batch* batch);
 /* Item positions x (np*3) and velocities v (np*3, may be NULL = 0), host or
  * device pointers. */
 int asg_batch_set_item(asg_batch* batch, int item, const float* x, const float* v, int device_ptrs);
+/* Run the items on `streams` concurrent streams (1..8, default 1): item i on
+ * stream i % streams, each stream with its own scratch (about 300 bytes per
+ * particle of the largest item), forked and joined inside the one graph. */
+int asg_batch_set_streams(asg_batch* batch, int streams);
 /* Optional autotuner: times the largest item with tree bucket sizes 16, 24, 32
  * and deposit work items of 2048, 4096, 8192 pairs and keeps the fastest. */
 int asg_batch_tune(asg_batch* batch, int* leaf, int* seg);

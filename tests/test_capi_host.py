@@ -43,7 +43,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_host_only_entry_points(lib):
-    assert lib.asg_abi_version() == 1
+    assert lib.asg_abi_version() == 2
     assert lib.asg_strerror(0) == b"ok"
     assert b"33" in lib.asg_strerror(-4)
     assert lib.asg_strerror(12345) == b"unknown status"

@@ -30,10 +30,12 @@ def smooth_ref(cube, ncs):
     return p, meshes, tot
 
 
-def test_batch_equals_smooth(batch_items):
+@pytest.mark.parametrize("streams", [1, 3])
+def test_batch_equals_smooth(batch_items, streams):
     items, ncs = batch_items
     assert len(items) == 6 and len({c.n for c in items}) > 1  # uneven counts
     with api.Context(0) as ctx, api.Batch(ctx, items, ncs) as b:
+        b.set_streams(streams)
         b.run()
         b.run()  # a replay of the captured graph
         st = b.stats()
