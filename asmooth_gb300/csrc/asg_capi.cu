@@ -42,6 +42,8 @@ struct MeshBuf {
 struct asg_ctx {
     int device = 0;
     cudaStream_t s = nullptr;
+    cudaStream_t s_out = nullptr;      // per-particle outputs copied out while the deposit runs
+    cudaEvent_t fields_ready = nullptr;
     int* d_err = nullptr;
     int* h_err = nullptr;  // pinned
     std::string last;
@@ -356,6 +358,8 @@ int asg_create(asg_ctx** out, int device)
     }
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fields_ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_u32, 4 * sizeof(uint32_t));
@@ -396,6 +400,11 @@ void asg_destroy(asg_ctx* ctx)
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
     if (ctx->h_u32) cudaFreeHost(ctx->h_u32);
     if (ctx->s) cudaStreamDestroy(ctx->s);
+    if (ctx->s_out) {
+        cudaStreamSynchronize(ctx->s_out);
+        cudaStreamDestroy(ctx->s_out);
+    }
+    if (ctx->fields_ready) cudaEventDestroy(ctx->fields_ready);
     delete ctx;
 }
 
@@ -1407,11 +1416,16 @@ int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, f
     build_index(ctx);
     run_knn(ctx);
     if (int r = queue_mark(ctx, halos, nh)) return r;
-    if (int r = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0)) return r;
+    // rk, dens and igrp are final: copy the records out while the deposit runs
+    CK(cudaEventRecord(ctx->fields_ready, ctx->s));
+    CK(cudaStreamWaitEvent(ctx->s_out, ctx->fields_ready, 0));
     launch_pack_aos(ctx->perm, P<float4>(ctx->pos), P<float4>(ctx->vel), P<float>(ctx->rk), nullptr,
-                    P<int>(ctx->igrp), np, ctx->aos.p, ctx->s);
+                    P<int>(ctx->igrp), np, ctx->aos.p, ctx->s_out);
     CK(cudaMemcpyAsync(p, ctx->aos.p, sizeof(asg_particle) * (size_t)np, cudaMemcpyDeviceToHost,
-                       ctx->s));
+                       ctx->s_out));
+    const int rd = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0);
+    CK(cudaStreamSynchronize(ctx->s_out));  // the records are in p before any return
+    if (rd) return rd;
     for (int k = 0; k < n_nc; ++k)
         if (meshes && meshes[k])
             CK(cudaMemcpyAsync(meshes[k], ctx->meshes[(size_t)k].mesh.p,
@@ -1443,14 +1457,19 @@ int asg_smooth_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off, con
     if (int r = stage_quant(ctx, cell, off, v, np, &dc, &doff, &dv)) return r;
     load_quant_device(ctx, dc, doff, dv, np, left, right, cell_size, grid);
     run_knn(ctx);
-    if (int r = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0)) return r;
-    // rk and dens back to input order; the particle arrays return in the same call
-    k_dens_of<<<(np + 255) / 256, 256, 0, ctx->s>>>(P<float4>(ctx->vel), np, P<float>(ctx->lab_scan));
+    // rk and dens are final: back to input order and out while the deposit runs
+    CK(cudaEventRecord(ctx->fields_ready, ctx->s));
+    CK(cudaStreamWaitEvent(ctx->s_out, ctx->fields_ready, 0));
+    k_dens_of<<<(np + 255) / 256, 256, 0, ctx->s_out>>>(P<float4>(ctx->vel), np,
+                                                         P<float>(ctx->lab_scan));
     count_launches(1);
     launch_scatter_fields(ctx->perm, P<float>(ctx->rk), P<float>(ctx->lab_scan), nullptr, np,
-                          P<float>(ctx->uf), P<float>(ctx->minin), nullptr, ctx->s);
-    if (rk) CK(cudaMemcpyAsync(rk, ctx->uf.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
-    if (dens) CK(cudaMemcpyAsync(dens, ctx->minin.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s));
+                          P<float>(ctx->uf), P<float>(ctx->minin), nullptr, ctx->s_out);
+    if (rk) CK(cudaMemcpyAsync(rk, ctx->uf.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s_out));
+    if (dens) CK(cudaMemcpyAsync(dens, ctx->minin.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s_out));
+    const int rd = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0);
+    CK(cudaStreamSynchronize(ctx->s_out));  // rk and dens are in place before any return
+    if (rd) return rd;
     for (int k = 0; k < n_nc; ++k)
         if (meshes && meshes[k])
             CK(cudaMemcpyAsync(meshes[k], ctx->meshes[(size_t)k].mesh.p,

@@ -11,7 +11,8 @@
 // Three warp-bundle traversals of the radix tree; a warp serves the 32
 // consecutive (Morton-ordered) particles of one bundle, one lane per particle,
 // and visits a node when any lane needs it:
-//   k_knn_t33   per-lane sorted top-33 of d2 in registers (min/max network)
+//   k_knn_t33   per-lane sorted top-33 of d2 in registers, candidates queued
+//               and merged by comparator networks (asg_knn_net.cuh)
 //               -> t33 = 33rd smallest d2 (exact, with multiplicity)
 //   k_knn_ties  exact-radius recount: L = #(d2 < t33), the tied indices
 //               -> idx33 = input index of the 33rd key, rk = sqrtf(t33)
@@ -23,25 +24,33 @@
 
 #include "asg_common.cuh"
 #include "asg_internal.h"
+#include "asg_knn_net.cuh"
 
 namespace asg {
 
 constexpr int KNN_WARPS = 4;
 constexpr unsigned FULL = 0xffffffffu;
 
-// min/max insertion of v into the ascending array a[FROM..32]; exact when
-// v >= a[FROM-1] (the lower slots would not change).  Returns the value that
-// drops out (the old a[32] when v < a[32]).
-template <int FROM>
-__device__ __forceinline__ float insert33_from(float (&a)[K_NN], float v)
+// Merges a lane's queued candidates (KNN_QUEUE values in shared memory, column
+// `lane`, +inf where unused) into its ascending top-33 a[] and refills the
+// queue with +inf.  tie_out ("a particle outside a[] has d2 == a[32]") stays
+// exact: the values dropped by the merge are all >= the 34th smallest t34, so
+// one of them ties the new a[32] exactly when t34 == a[32]; an earlier tie
+// survives only while a[32] is unchanged.
+__device__ __forceinline__ void knn_flush(float (&a)[K_NN], float* qb, int& qn, bool& tie_out)
 {
+    float v[KNN_QUEUE];
 #pragma unroll
-    for (int k = FROM; k < K_NN; ++k) {
-        const float lo = fminf(a[k], v);
-        v = fmaxf(a[k], v);
-        a[k] = lo;
+    for (int i = 0; i < KNN_QUEUE; ++i) {
+        v[i] = qb[32 * i];
+        qb[32 * i] = INFINITY;
     }
-    return v;
+    qn = 0;
+    knn_sort16(v);
+    const float old = a[K_NN - 1];
+    const float t34 = knn_merge33(a, v);
+    const float top = a[K_NN - 1];
+    tie_out = (top == old && tie_out) || t34 == top;
 }
 
 // squared distance from the query to a child (point for a leaf child)
@@ -58,15 +67,19 @@ __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, con
 // t33 = the 33rd smallest d2 (with multiplicity), rk = sqrtf(t33), and a tie
 // flag: idx33 = -1 when exactly one particle sits at d2 == t33 (then the
 // 32-set is {d2 < t33} and needs no index), -2 when ties must be resolved.
-// The flag tracks whether any particle outside the kept 33 has d2 equal to
-// the current 33rd value: rejected candidates with d2 == a[32], and evicted
-// values equal to the new a[32]; it is cleared whenever a[32] decreases.
-__global__ void __launch_bounds__(KNN_WARPS * 32, 8)
+// Each lane keeps its 33 smallest d2 sorted in registers; a candidate with
+// d2 <= a[32] goes to the lane's queue in shared memory, and when any lane's
+// queue is full the warp merges every queue with two comparator networks
+// (sort the queue, odd-even merge with a[]), about a quarter of the min/max
+// work of inserting each candidate as it comes.  Thresholds are the merged
+// a[32], an upper bound of the true one while values wait in the queue.
+__global__ void __launch_bounds__(KNN_WARPS * 32, 6)
 k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
           float* __restrict__ rk, int* __restrict__ idx33, int* err)
 {
     __shared__ int stk[KNN_WARPS][STACK_MAX];
     __shared__ float4 cand[KNN_WARPS][32];
+    __shared__ float queue[KNN_WARPS][KNN_QUEUE][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = t.n;
     const int base = (blockIdx.x * KNN_WARPS + warp) * 32;
@@ -77,6 +90,10 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
 #pragma unroll
     for (int k = 0; k < K_NN; ++k) a[k] = INFINITY;
     bool tie_out = false;  // a particle outside a[] has d2 == a[32]
+    float* qb = &queue[warp][0][lane];
+    int qn = 0;
+#pragma unroll
+    for (int i = 0; i < KNN_QUEUE; ++i) qb[32 * i] = INFINITY;
 
     int* st = stk[warp];
     if (lane == 0) st[0] = tree_root(n);
@@ -121,18 +138,15 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
         for (int j = 0; j < cnt; ++j) {
             const float4 c = cand[warp][j];
             const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
-            const float top = a[K_NN - 1];
-            const bool take = d2 < top;
-            tie_out |= (d2 == top);
-            if (__any_sync(FULL, take)) {
-                insert33_from<0>(a, take ? d2 : INFINITY);
-                // the value that dropped out is the old a[32]: a tie remains exactly
-                // when the new a[32] still equals it
-                if (take) tie_out = (a[K_NN - 1] == top);
+            if (d2 <= a[K_NN - 1]) {  // equal values queue too: the merge tracks ties
+                qb[32 * qn] = d2;
+                ++qn;
             }
+            if (__any_sync(FULL, qn == KNN_QUEUE)) knn_flush(a, qb, qn, tie_out);
         }
         __syncwarp();
     }
+    if (__any_sync(FULL, qn > 0)) knn_flush(a, qb, qn, tie_out);
     if (overflow) {
         if (lane == 0) atomicOr(err, ERR_STACK);
         return;

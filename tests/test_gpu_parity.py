@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import pyoracle as po
-from helpers import exact_t33, rel_err_cells, set_from_key
+from helpers import dens_brute, exact_t33, rel_err_cells, set_from_key
 
 from asmooth_gb300 import api
 from asmooth_gb300 import synthetic as syn
@@ -61,7 +61,7 @@ def test_neighbor_search_golden(gpu_ctx, golden, oracle):
     t33, idx33 = gpu_ctx.get_knn(len(x))
     for q, ref in zip(g["nbr_sample"], g["nbr"]):
         assert np.array_equal(set_from_key(x, int(q), t33[q], idx33[q]), ref)
-    # dens: reference float sums in kd-tree order vs our fixed-order double-float sums
+    # dens: the reference's float sums in kd-tree order vs our exact fixed-point sums
     assert np.max(np.abs(p["dens"] - g["dens"]) / g["dens"]) <= FIELD_TOL
     te, ie, nbr = oracle.knn_exact(x, g["left"], g["right"], NTHREADS)
     assert np.array_equal(bits(te), bits(t33)) and np.array_equal(ie, idx33)
@@ -225,6 +225,10 @@ def test_full_size_cfg2_properties(gpu_ctx):
         t, k = exact_t33(x, int(q))
         assert t == t33[q] and k == idx33[q]
         assert p["rk"][q] == np.sqrt(np.float32(t))
+    # dens of sampled receivers against a brute-force sum over all 18.3 M queries
+    for j in rng.choice(cube.n, 16, replace=False):
+        s = dens_brute(x, p["rk"], t33, idx33, int(j))
+        assert abs(float(p["dens"][j]) - s) <= FIELD_TOL * s
     for k, nc in enumerate(ncs):
         assert 0.999 < tot1[k].sum() / cube.n_local < 1.001
 
