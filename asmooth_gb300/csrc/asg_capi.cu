@@ -71,7 +71,8 @@ struct asg_ctx {
     int dec_n = 0;          // particles of the last decode (in sh_in), 0 = none
     uint32_t dep_npairs = 0;
     int dep_tiles_n = 0;
-    uint32_t* h_u32 = nullptr;  // pinned
+    uint32_t* h_u32 = nullptr;      // pinned, mapped
+    uint32_t* h_u32_dev = nullptr;  // its device address
     float mesh_boxsize = 0.0f;
     std::vector<MeshBuf> meshes;
 
@@ -164,6 +165,24 @@ void phase_end(asg_ctx* ctx)
     cudaEventRecord(e, ctx->s);
     ctx->pending.push_back({ctx->open_phase, {ctx->open_ev, e}});
     ctx->open_phase = -1;
+}
+
+// Reads one or two device words into ctx->h_u32 and waits for them.  A kernel
+// stores them through the mapped host words: a copy would queue on the copy
+// engine behind any large device-to-host copy in flight on another stream.
+__global__ void k_read_words(const uint32_t* a, const uint32_t* b, uint32_t* out)
+{
+    out[0] = *a;
+    if (b) out[1] = *b;
+}
+
+static int read_words(asg_ctx* ctx, const uint32_t* a, const uint32_t* b = nullptr)
+{
+    k_read_words<<<1, 1, 0, ctx->s>>>(a, b, ctx->h_u32_dev);
+    count_launches(1);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->s));
+    return 0;
 }
 
 // wait for the queued work and report device-side and launch errors
@@ -362,7 +381,8 @@ int asg_create(asg_ctx** out, int device)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fields_ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_err, sizeof(int));
-    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_u32, 4 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaHostAlloc(&ctx->h_u32, 4 * sizeof(uint32_t), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(&ctx->h_u32_dev, ctx->h_u32, 0);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->s);
     if (e != cudaSuccess) {
@@ -499,9 +519,7 @@ static int load_shell(asg_ctx* ctx, int np, float boxsize, float bf, int* np_wit
                         reinterpret_cast<int*>(a + o_igrp), reinterpret_cast<float*>(a + o_rk),
                         n_all, -dx, boxsize + dx, flags, a + o_scan, P<float4>(ctx->pos_in),
                         P<float4>(ctx->vel_in), P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->s);
-    CK(cudaMemcpyAsync(ctx->h_u32, flags + n_all, 4, cudaMemcpyDeviceToHost, ctx->s));
-    CK(cudaMemcpyAsync(ctx->h_u32 + 1, flags + np, 4, cudaMemcpyDeviceToHost, ctx->s));
-    CK(cudaStreamSynchronize(ctx->s));
+    if (int r = read_words(ctx, flags + n_all, flags + np)) return r;
     const int n = (int)ctx->h_u32[0];
     if (np_with) *np_with = n;
     if (np_local) *np_local = (int)ctx->h_u32[1];
@@ -1002,8 +1020,7 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
                         P<float>(ctx->rk), n, p, w, ctx->d_err, ctx->s);
     uint32_t npairs = cap;
     if (!cap) {
-        CK(cudaMemcpyAsync(ctx->h_u32, w.pcount + n, 4, cudaMemcpyDeviceToHost, ctx->s));
-        CK(cudaStreamSynchronize(ctx->s));
+        if (int r = read_words(ctx, w.pcount + n)) return r;
         npairs = ctx->h_u32[0];
     }
     const size_t NP = (size_t)npairs + 1;

@@ -73,7 +73,7 @@ __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, con
 // (sort the queue, odd-even merge with a[]), about a quarter of the min/max
 // work of inserting each candidate as it comes.  Thresholds are the merged
 // a[32], an upper bound of the true one while values wait in the queue.
-__global__ void __launch_bounds__(KNN_WARPS * 32, 6)
+__global__ void __launch_bounds__(KNN_WARPS * 32, 8)
 k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
           float* __restrict__ rk, int* __restrict__ idx33, int* err)
 {
