@@ -61,6 +61,7 @@ struct asg_ctx {
     Buf pos, vel, igrp, rk, t33, idx33;
     Buf meta, parent, leaf_parent, flags, blo, bhi;
     Buf dacc, dexp;  // dens: fixed-point sums and scale exponents
+    Buf blist;       // buckets each bundle's neighbour search scanned
     Buf uf, minin, mark, scan_tmp, lab_cnt, lab_scan;
     Buf halos, hcount, hmass;
     Buf totals, lohi;
@@ -248,6 +249,7 @@ int alloc_set(asg_ctx* ctx, int n)
     r |= grow(ctx, ctx->bhi, 16 * M);
     r |= grow(ctx, ctx->dacc, 8 * N);
     r |= grow(ctx, ctx->dexp, 4 * N);
+    r |= grow(ctx, ctx->blist, 4 * knn_list_words(n));
     return r ? ASG_ERR_NOMEM : 0;
 }
 
@@ -403,7 +405,7 @@ void asg_destroy(asg_ctx* ctx)
                    &ctx->keys0, &ctx->keys1, &ctx->vals0, &ctx->vals1, &ctx->sort_tmp,
                    &ctx->pos, &ctx->vel, &ctx->igrp, &ctx->rk, &ctx->t33, &ctx->idx33,
                    &ctx->meta, &ctx->parent, &ctx->leaf_parent, &ctx->flags, &ctx->blo,
-                   &ctx->bhi, &ctx->dacc, &ctx->dexp, &ctx->uf, &ctx->minin, &ctx->mark,
+                   &ctx->bhi, &ctx->dacc, &ctx->dexp, &ctx->blist, &ctx->uf, &ctx->minin, &ctx->mark,
                    &ctx->scan_tmp, &ctx->lab_cnt, &ctx->lab_scan, &ctx->halos, &ctx->hcount,
                    &ctx->hmass, &ctx->totals, &ctx->lohi, &ctx->dep_rec, &ctx->dep_pcount,
                    &ctx->dep_tiles, &ctx->dep_counter, &ctx->dep_pairs, &ctx->dep_sort,
@@ -812,7 +814,7 @@ static int run_knn(asg_ctx* ctx)
     const TreeView t = tree_view(ctx);
     phase_begin(ctx, ASG_PH_KNN);
     launch_knn_t33(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<float>(ctx->rk),
-                   P<int>(ctx->idx33), ctx->d_err, ctx->s);
+                   P<int>(ctx->idx33), P<int>(ctx->blist), ctx->d_err, ctx->s);
     phase_end(ctx);
     phase_begin(ctx, ASG_PH_TIES);  // only bundles with an exact tie at the 33rd distance
     launch_knn_ties(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33), 0,
@@ -822,8 +824,9 @@ static int run_knn(asg_ctx* ctx)
     ctx->rk_checked = false;
     ensure_rk_checked(ctx);
     phase_begin(ctx, ASG_PH_DENS);
-    launch_dens(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33), P<float>(ctx->rk),
-                P<int>(ctx->dexp), P<unsigned long long>(ctx->dacc), P<float4>(ctx->vel), ctx->s);
+    launch_dens(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33), P<int>(ctx->blist),
+                P<float>(ctx->rk), P<int>(ctx->dexp), P<unsigned long long>(ctx->dacc),
+                P<float4>(ctx->vel), ctx->s);
     phase_end(ctx);
     ctx->knn_done = true;
     return 0;

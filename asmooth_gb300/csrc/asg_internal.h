@@ -74,16 +74,23 @@ size_t scan_temp_bytes(size_t n);
 void exclusive_scan_u32(uint32_t* data, size_t n, void* temp, cudaStream_t s);
 
 // ---- neighbour search (asg_knn.cu) -------------------------------------------
-// t33, rk = sqrtf(t33), idx33 = -1 (no tie at the 33rd) or -2 (ties to resolve)
+// Buckets k_knn_t33 scanned, per 32-query bundle: word 0 = their count (-1 when
+// more than KNN_LIST), then the node ids (a bucket node, or ~i for one particle).
+// k_dens_scatter visits these instead of walking the tree again.
+constexpr int KNN_LIST = 96;
+inline size_t knn_list_words(int n) { return (size_t)((n + 31) / 32) * (KNN_LIST + 1); }
+// t33, rk = sqrtf(t33), idx33 = -1 (no tie at the 33rd) or -2 (ties to resolve);
+// blist (knn_list_words ints, or null) receives the scanned buckets
 void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, float* rk, int* idx33,
-                    int* err, cudaStream_t s);
+                    int* blist, int* err, cudaStream_t s);
 // idx33 = input index of the 33rd key, for flagged queries (all = 0) or every query
 void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int* idx33,
                      int all, int* err, cudaStream_t s);
 // vel[j].w (dens) += the tent weights j receives as one of the 32 nearest;
-// dexp (n ints) and acc (n uint64) are scratch
+// dexp (n ints) and acc (n uint64) are scratch; blist from launch_knn_t33 or null
 void launch_dens(const float4* pos, const TreeView& t, const float* t33, const int* idx33,
-                 const float* rk, int* dexp, unsigned long long* acc, float4* vel, cudaStream_t s);
+                 const int* blist, const float* rk, int* dexp, unsigned long long* acc,
+                 float4* vel, cudaStream_t s);
 
 // ---- mesh deposit (asg_deposit.cu) ---------------------------------------------
 struct MeshJob {

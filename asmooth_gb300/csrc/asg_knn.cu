@@ -75,7 +75,7 @@ __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, con
 // a[32], an upper bound of the true one while values wait in the queue.
 __global__ void __launch_bounds__(KNN_WARPS * 32, 8)
 k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
-          float* __restrict__ rk, int* __restrict__ idx33, int* err)
+          float* __restrict__ rk, int* __restrict__ idx33, int* __restrict__ blist, int* err)
 {
     __shared__ int stk[KNN_WARPS][STACK_MAX];
     __shared__ float4 cand[KNN_WARPS][32];
@@ -94,6 +94,8 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
     int qn = 0;
 #pragma unroll
     for (int i = 0; i < KNN_QUEUE; ++i) qb[32 * i] = INFINITY;
+    __shared__ int nlist[KNN_WARPS];  // buckets scanned (kept in shared memory: registers are full)
+    if (lane == 0) nlist[warp] = 0;
 
     int* st = stk[warp];
     if (lane == 0) st[0] = tree_root(n);
@@ -132,6 +134,11 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             const float db = box_dist2_rn(xq.x, xq.y, xq.z, t.blo[node], t.bhi[node]);
             if (!__any_sync(FULL, db <= a[K_NN - 1])) continue;
         }
+        if (blist && lane == 0) {
+            const int k = nlist[warp];
+            if (k < KNN_LIST) blist[(size_t)(base >> 5) * (KNN_LIST + 1) + 1 + k] = node;
+            nlist[warp] = k + 1;
+        }
         const int cnt = last - first + 1;
         if (lane < cnt) cand[warp][lane] = pos[first + lane];
         __syncwarp();
@@ -147,6 +154,11 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
         __syncwarp();
     }
     if (__any_sync(FULL, qn > 0)) knn_flush(a, qb, qn, tie_out);
+    // every bucket any lane's final radius reaches was scanned, so the list is
+    // complete for k_dens_scatter unless it overflowed or the stack did
+    if (blist && lane == 0)
+        blist[(size_t)(base >> 5) * (KNN_LIST + 1)] =
+            (overflow || nlist[warp] > KNN_LIST) ? -1 : nlist[warp];
     if (overflow) {
         if (lane == 0) atomicOr(err, ERR_STACK);
         return;
@@ -271,13 +283,16 @@ __global__ void k_dens_prep(const float* __restrict__ rk, int n, int* __restrict
 }
 
 // Each lane is a query q with its exact radius: it visits the candidates j
-// with d2 <= t33_q (the exact-radius traversal of k_knn_ties), and for every j
-// of its 32-set (d2 < t33, or d2 == t33 with index below idx33) the warp adds
-// the members' fixed-point weights and one lane adds the sum to acc[j].
+// with d2 <= t33_q, and for every j of its 32-set (d2 < t33, or d2 == t33 with
+// index below idx33) the warp adds the members' fixed-point weights and one
+// lane adds the sum to acc[j].  The buckets come from the bundle's list of
+// buckets k_knn_t33 scanned (each re-tested against the exact radii), or from
+// a walk of the tree when the list overflowed or is absent.
 __global__ void __launch_bounds__(KNN_WARPS * 32)
 k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
-               const int* __restrict__ idx33, const float* __restrict__ rk,
-               const int* __restrict__ dexp, unsigned long long* __restrict__ acc)
+               const int* __restrict__ idx33, const int* __restrict__ blist,
+               const float* __restrict__ rk, const int* __restrict__ dexp,
+               unsigned long long* __restrict__ acc)
 {
     __shared__ int stk[KNN_WARPS][STACK_MAX];
     __shared__ float4 cand[KNN_WARPS][32];
@@ -293,6 +308,57 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
     const int i33 = idx33[q];
     const float hinv = __fdiv_rn(1.0f, rk[q]);
     const bool any_tie = __any_sync(FULL, valid && i33 >= 0);  // warp-uniform
+
+    // scans bucket [first, last] against every lane's 32-set
+    auto scan = [&](int first, int last) {
+        const int cnt = last - first + 1;
+        if (lane < cnt) {
+            cand[warp][lane] = pos[first + lane];
+            cscale[warp][lane] = __int_as_float((127 + FIX_BITS - dexp[first + lane]) << 23);
+        }
+        __syncwarp();
+        for (int k = 0; k < cnt; ++k) {
+            const float4 c = cand[warp][k];
+            const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
+            // the index rule matters only where the 33rd distance is tied
+            const bool member = d2 < T || (any_tie && d2 == T && __float_as_int(c.w) < i33);
+            if (__any_sync(FULL, member)) {
+                const float w = member ? ker_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z, hinv) : 0.0f;
+                const unsigned long long f = __float2ull_rn(__fmul_rn(w, cscale[warp][k]));
+                const unsigned s0 = __reduce_add_sync(FULL, (unsigned)(f & 0x3fffffull));
+                const unsigned s1 = __reduce_add_sync(FULL, (unsigned)(f >> 22));
+                if (lane == 0)
+                    atomicAdd(&acc[first + k], (unsigned long long)s0 + ((unsigned long long)s1 << 22));
+            }
+        }
+        __syncwarp();
+    };
+
+    const int* bl = blist ? blist + (size_t)(base >> 5) * (KNN_LIST + 1) : nullptr;
+    const int nlist = bl ? bl[0] : -1;
+    if (nlist >= 0) {
+        // the list in registers: entry i in lane i & 31 of word i >> 5
+        int e[(KNN_LIST + 31) / 32];
+#pragma unroll
+        for (int w = 0; w < (KNN_LIST + 31) / 32; ++w)
+            e[w] = 32 * w + lane < nlist ? bl[1 + 32 * w + lane] : 0;
+        for (int i = 0; i < nlist; ++i) {
+            int v = e[0];
+#pragma unroll
+            for (int w = 1; w < (KNN_LIST + 31) / 32; ++w)
+                if ((i >> 5) == w) v = e[w];
+            const int node = __shfl_sync(FULL, v, i & 31);
+            if (node < 0) {
+                scan(~node, ~node);
+                continue;
+            }
+            const float db = box_dist2_rn(xq.x, xq.y, xq.z, t.blo[node], t.bhi[node]);
+            if (!__any_sync(FULL, db <= T)) continue;
+            const int4 m = t.meta[node];
+            scan(m.z, m.w);
+        }
+        return;
+    }
 
     int* st = stk[warp];
     if (lane == 0) st[0] = tree_root(n);
@@ -321,27 +387,7 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
             first = m.z;
             last = m.w;
         }
-        const int cnt = last - first + 1;
-        if (lane < cnt) {
-            cand[warp][lane] = pos[first + lane];
-            cscale[warp][lane] = __int_as_float((127 + FIX_BITS - dexp[first + lane]) << 23);
-        }
-        __syncwarp();
-        for (int k = 0; k < cnt; ++k) {
-            const float4 c = cand[warp][k];
-            const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
-            // the index rule matters only where the 33rd distance is tied
-            const bool member = d2 < T || (any_tie && d2 == T && __float_as_int(c.w) < i33);
-            if (__any_sync(FULL, member)) {
-                const float w = member ? ker_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z, hinv) : 0.0f;
-                const unsigned long long f = __float2ull_rn(__fmul_rn(w, cscale[warp][k]));
-                const unsigned s0 = __reduce_add_sync(FULL, (unsigned)(f & 0x3fffffull));
-                const unsigned s1 = __reduce_add_sync(FULL, (unsigned)(f >> 22));
-                if (lane == 0)
-                    atomicAdd(&acc[first + k], (unsigned long long)s0 + ((unsigned long long)s1 << 22));
-            }
-        }
-        __syncwarp();
+        scan(first, last);
     }
 }
 
@@ -361,10 +407,10 @@ __global__ void k_dens_finish(const unsigned long long* __restrict__ acc,
 static int knn_blocks(int n) { return (n + KNN_WARPS * 32 - 1) / (KNN_WARPS * 32); }
 
 void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, float* rk, int* idx33,
-                    int* err, cudaStream_t s)
+                    int* blist, int* err, cudaStream_t s)
 {
     if (t.n <= 0) return;
-    k_knn_t33<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, rk, idx33, err);
+    k_knn_t33<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, rk, idx33, blist, err);
     count_launches(1);
 }
 
@@ -377,12 +423,14 @@ void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int
 }
 
 void launch_dens(const float4* pos, const TreeView& t, const float* t33, const int* idx33,
-                 const float* rk, int* dexp, unsigned long long* acc, float4* vel, cudaStream_t s)
+                 const int* blist, const float* rk, int* dexp, unsigned long long* acc,
+                 float4* vel, cudaStream_t s)
 {
     if (t.n <= 0) return;
     const int nb = (t.n + 255) / 256;
     k_dens_prep<<<nb, 256, 0, s>>>(rk, t.n, dexp, acc);
-    k_dens_scatter<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, rk, dexp, acc);
+    k_dens_scatter<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, blist, rk, dexp,
+                                                             acc);
     k_dens_finish<<<nb, 256, 0, s>>>(acc, dexp, t.n, vel);
     count_launches(3);
 }

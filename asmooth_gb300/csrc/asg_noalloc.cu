@@ -179,10 +179,10 @@ extern "C" int asg_neighbor_search_noalloc(const float* d_x, int np, float left,
     t.meta = reinterpret_cast<const int4*>(b + L.meta);
     t.blo = F4(L.blo);
     t.bhi = F4(L.bhi);
-    launch_knn_t33(F4(L.pos), t, F(L.t33), F(L.rk), I(L.idx33), err, s);
+    launch_knn_t33(F4(L.pos), t, F(L.t33), F(L.rk), I(L.idx33), nullptr, err, s);
     launch_knn_ties(F4(L.pos), t, F(L.t33), I(L.idx33), 0, err, s);
     launch_check_rk(F(L.rk), np, err, s);
-    launch_dens(F4(L.pos), t, F(L.t33), I(L.idx33), F(L.rk), I(L.dexp),
+    launch_dens(F4(L.pos), t, F(L.t33), I(L.idx33), nullptr, F(L.rk), I(L.dexp),
                 reinterpret_cast<unsigned long long*>(b + L.dacc), F4(L.vel), s);
     k_noalloc_store<<<(np + 255) / 256, 256, 0, s>>>(perm, F(L.rk), F4(L.vel), np, d_rk, d_dens);
     count_launches(1);
