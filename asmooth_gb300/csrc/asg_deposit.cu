@@ -265,20 +265,19 @@ __device__ __forceinline__ int tile_slot(int x, int y, int z)
     return (z << 6) | (y << 3) | ((x + 6 * y + 4 * z) & (TS - 1));
 }
 
-// 1/d rounded to nearest, d = 0..64: floor(c / d) = trunc((c + 0.5) * (1/d))
-// exactly for 0 <= c < 4096 (checked for every c and d in float32)
-#define ASG_R(d) (1.0f / (float)(d))
-#define ASG_R8(b) ASG_R(b + 1), ASG_R(b + 2), ASG_R(b + 3), ASG_R(b + 4), ASG_R(b + 5), \
-    ASG_R(b + 6), ASG_R(b + 7), ASG_R(b + 8)
-__constant__ float c_rcp[TS * TS + 1] = {0.0f, ASG_R8(0), ASG_R8(8), ASG_R8(16), ASG_R8(24),
-                                         ASG_R8(32), ASG_R8(40), ASG_R8(48), ASG_R8(56)};
-#undef ASG_R8
-#undef ASG_R
+// floor(c / d) = (c * m_d) >> 15 with m_d = ceil(2^15 / d), exactly for
+// 0 <= c < 512 and 1 <= d <= 64 (checked for every c and d): a pair's box has
+// at most 8^3 cells and nx * ny <= 64.  Integer multiply and shift, no
+// conversions on the per-cell path.
+#define ASG_M15(d) ((32768 + (d) - 1) / (d))
+#define ASG_M8(b) ASG_M15(b + 1), ASG_M15(b + 2), ASG_M15(b + 3), ASG_M15(b + 4), \
+    ASG_M15(b + 5), ASG_M15(b + 6), ASG_M15(b + 7), ASG_M15(b + 8)
+__constant__ int c_m15[TS * TS + 1] = {0, ASG_M8(0), ASG_M8(8), ASG_M8(16), ASG_M8(24),
+                                       ASG_M8(32), ASG_M8(40), ASG_M8(48), ASG_M8(56)};
+#undef ASG_M8
+#undef ASG_M15
 
-__device__ __forceinline__ int small_div(int c, float rcp)
-{
-    return __float2int_rz(__fmul_rn(__fadd_rn(__int2float_rn(c), 0.5f), rcp));
-}
+__device__ __forceinline__ int small_div(int c, int m) { return (c * m) >> 15; }
 
 // one particle's weight w3 into one cell: n and c as double-float, v as float
 __device__ __forceinline__ void add_cell(WarpTile& S, int slot, float w3, float dens, float vx,
@@ -437,9 +436,11 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                         const int sh = k * nc + g.O[a];
                         const int r0 = max(ar.left - sh, 0), r1 = min(ar.right - sh, g.E[a]);
                         r |= (uint32_t)((r0 & 15) | ((max(r1, r0) & 15) << 4)) << (8 * a);
-                        for (int t = r0; t < r1; ++t) {
-                            const int ii = t + sh;  // unwrapped cell index
-                            const float s1 = __fmul_rn(__fsub_rn(__fmul_rn((float)ii, J.dx), xs[a]), hinv);
+                        // (float) of the unwrapped cell index t + sh, stepped by exact float
+                        // additions (|index| < 2^24) instead of one conversion per cell
+                        float fi = (float)(r0 + sh);
+                        for (int t = r0; t < r1; ++t, fi = __fadd_rn(fi, 1.0f)) {
+                            const float s1 = __fmul_rn(__fsub_rn(__fmul_rn(fi, J.dx), xs[a]), hinv);
                             wl[a * TS + t] = ker_integ_rn(s1, __fadd_rn(s1, ds));
                         }
                     }
@@ -461,7 +462,7 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                 const float vy = __shfl_sync(FULLM, val.z, p);
                 const float vz = __shfl_sync(FULLM, val.w, p);
                 const int nxy = nx * ny, ncell = nxy * nz;
-                const float rx = c_rcp[nx], rxy = c_rcp[nxy];
+                const int rx = c_m15[nx], rxy = c_m15[nxy];
                 const float* wp = S.w[p];
                 const bool hal = (rp >> 24) != 0;
                 if (!hal) {
