@@ -140,16 +140,21 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             nlist[warp] = k + 1;
         }
         const int cnt = last - first + 1;
+        // an odd bucket is padded with a NaN point, whose distance queues nowhere
         if (lane < cnt) cand[warp][lane] = pos[first + lane];
+        else if (lane == cnt) cand[warp][lane] = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
         __syncwarp();
-        for (int j = 0; j < cnt; ++j) {
-            const float4 c = cand[warp][j];
-            const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
-            if (d2 <= a[K_NN - 1]) {  // equal values queue too: the merge tracks ties
-                qb[32 * qn] = d2;
-                ++qn;
-            }
-            if (__any_sync(FULL, qn == KNN_QUEUE)) knn_flush(a, qb, qn, tie_out);
+        // two candidates per step, then one check: every queue holds at most
+        // KNN_QUEUE - 2 values when a step begins (equal values queue too: the
+        // merge tracks ties)
+        for (int j = 0; j < cnt; j += 2) {
+            const float4 c0 = cand[warp][j], c1 = cand[warp][j + 1];
+            const float d0 = norm2_rn(xq.x, xq.y, xq.z, c0.x, c0.y, c0.z);
+            const float d1 = norm2_rn(xq.x, xq.y, xq.z, c1.x, c1.y, c1.z);
+            const float top = a[K_NN - 1];
+            if (d0 <= top) qb[32 * qn++] = d0;
+            if (d1 <= top) qb[32 * qn++] = d1;
+            if (__any_sync(FULL, qn > KNN_QUEUE - 2)) knn_flush(a, qb, qn, tie_out);
         }
         __syncwarp();
     }
