@@ -62,6 +62,7 @@ struct asg_ctx {
     Buf meta, parent, leaf_parent, flags, blo, bhi;
     Buf dacc, dexp;  // dens: fixed-point sums and scale exponents
     Buf blist;       // buckets each bundle's neighbour search scanned
+    Buf nrec;        // tree node records (TreeView::rec)
     Buf uf, minin, mark, scan_tmp, lab_cnt, lab_scan;
     Buf halos, hcount, hmass;
     Buf totals, lohi;
@@ -219,6 +220,7 @@ TreeView tree_view(asg_ctx* ctx)
     t.meta = P<int4>(ctx->meta);
     t.blo = P<float4>(ctx->blo);
     t.bhi = P<float4>(ctx->bhi);
+    t.rec = P<float4>(ctx->nrec);
     return t;
 }
 
@@ -247,6 +249,7 @@ int alloc_set(asg_ctx* ctx, int n)
     r |= grow(ctx, ctx->flags, 4 * M);
     r |= grow(ctx, ctx->blo, 16 * M);
     r |= grow(ctx, ctx->bhi, 16 * M);
+    r |= grow(ctx, ctx->nrec, 64 * M);
     r |= grow(ctx, ctx->dacc, 8 * N);
     r |= grow(ctx, ctx->dexp, 4 * N);
     r |= grow(ctx, ctx->blist, 4 * knn_list_words(n));
@@ -269,6 +272,8 @@ int build_index(asg_ctx* ctx)
     launch_tree_boxes(P<float4>(ctx->pos), nullptr, n, ctx->leaf, P<int4>(ctx->meta),
                       P<int>(ctx->parent), P<int>(ctx->flags), P<float4>(ctx->blo),
                       P<float4>(ctx->bhi), ctx->s);
+    launch_tree_records(P<float4>(ctx->pos), n, ctx->leaf, P<int4>(ctx->meta), P<float4>(ctx->blo),
+                        P<float4>(ctx->bhi), P<float4>(ctx->nrec), ctx->s);
     phase_end(ctx);
     ctx->loaded = true;
     ctx->knn_done = false;
@@ -405,7 +410,7 @@ void asg_destroy(asg_ctx* ctx)
                    &ctx->keys0, &ctx->keys1, &ctx->vals0, &ctx->vals1, &ctx->sort_tmp,
                    &ctx->pos, &ctx->vel, &ctx->igrp, &ctx->rk, &ctx->t33, &ctx->idx33,
                    &ctx->meta, &ctx->parent, &ctx->leaf_parent, &ctx->flags, &ctx->blo,
-                   &ctx->bhi, &ctx->dacc, &ctx->dexp, &ctx->blist, &ctx->uf, &ctx->minin, &ctx->mark,
+                   &ctx->bhi, &ctx->dacc, &ctx->dexp, &ctx->blist, &ctx->nrec, &ctx->uf, &ctx->minin, &ctx->mark,
                    &ctx->scan_tmp, &ctx->lab_cnt, &ctx->lab_scan, &ctx->halos, &ctx->hcount,
                    &ctx->hmass, &ctx->totals, &ctx->lohi, &ctx->dep_rec, &ctx->dep_pcount,
                    &ctx->dep_tiles, &ctx->dep_counter, &ctx->dep_pairs, &ctx->dep_sort,

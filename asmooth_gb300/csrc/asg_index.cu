@@ -571,6 +571,47 @@ void launch_tree_boxes(const float4* pos, const float* rk, int n, int leaf, cons
     count_launches(1);
 }
 
+// one 64-byte record per internal node (see TreeView::rec); a bucket nested
+// inside a larger bucket has no box and is never visited, so its record is
+// never read
+__global__ void k_tree_records(const float4* __restrict__ pos, int n, int leaf,
+                               const int4* __restrict__ meta, const float4* __restrict__ lo,
+                               const float4* __restrict__ hi, float4* __restrict__ rec)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int4 m = meta[i];
+    float4 a, b;
+    float4 r1, r2, r3 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (m.w - m.z + 1 > leaf) {
+        float4 l0, h0, l1, h1;
+        if (m.x < 0) l0 = h0 = pos[~m.x]; else { l0 = lo[m.x]; h0 = hi[m.x]; }
+        if (m.y < 0) l1 = h1 = pos[~m.y]; else { l1 = lo[m.y]; h1 = hi[m.y]; }
+        r1 = make_float4(l0.x, l0.y, l0.z, h0.x);
+        r2 = make_float4(h0.y, h0.z, l1.x, l1.y);
+        r3 = make_float4(l1.z, h1.x, h1.y, h1.z);
+    } else {
+        a = lo[i];
+        b = hi[i];
+        r1 = make_float4(a.x, a.y, a.z, b.x);
+        r2 = make_float4(b.y, b.z, 0.f, 0.f);
+    }
+    float4* r = rec + 4 * (size_t)i;
+    r[0] = make_float4(__int_as_float(m.x), __int_as_float(m.y), __int_as_float(m.z),
+                       __int_as_float(m.w));
+    r[1] = r1;
+    r[2] = r2;
+    r[3] = r3;
+}
+
+void launch_tree_records(const float4* pos, int n, int leaf, const int4* meta, const float4* lo,
+                         const float4* hi, float4* rec, cudaStream_t s)
+{
+    if (n <= 1) return;
+    k_tree_records<<<(n - 1 + 255) / 256, 256, 0, s>>>(pos, n, leaf, meta, lo, hi, rec);
+    count_launches(1);
+}
+
 // ---------------------------------------------------------------------------
 // output in input order
 // ---------------------------------------------------------------------------

@@ -27,6 +27,12 @@ struct TreeView {
     const int4* meta;      // internal nodes 0..n-2 (root 0); empty when n == 1
     const float4* blo;
     const float4* bhi;
+    // 64 bytes per internal node, one load round trip per visit: word 0 the
+    // meta (c0, c1, first, last as int bits); words 1-3 the boxes of both
+    // children of a node with more than `leaf` particles (a leaf child as its
+    // point: lo0.xyz hi0.x | hi0.yz lo1.xy | lo1.z hi1.xyz), or the node's own
+    // box for a bucket (lo.xyz hi.x | hi.yz)
+    const float4* rec;
 };
 
 // root entry of a traversal: internal node 0, or leaf 0 when n == 1
@@ -69,6 +75,9 @@ void launch_build_tree(const uint64_t* keys, int n, int4* meta, int* parent, int
 // rk != nullptr the expanded boxes [x-h', x+h']
 void launch_tree_boxes(const float4* pos, const float* rk, int n, int leaf, const int4* meta,
                        const int* parent, int* flags, float4* lo, float4* hi, cudaStream_t s);
+// TreeView::rec from meta and the boxes (4 float4 per internal node)
+void launch_tree_records(const float4* pos, int n, int leaf, const int4* meta, const float4* lo,
+                         const float4* hi, float4* rec, cudaStream_t s);
 // exclusive scan of uint32 counts (in place); temp from scan_temp_bytes
 size_t scan_temp_bytes(size_t n);
 void exclusive_scan_u32(uint32_t* data, size_t n, void* temp, cudaStream_t s);

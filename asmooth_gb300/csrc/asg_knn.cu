@@ -53,6 +53,18 @@ __device__ __forceinline__ void knn_flush(float (&a)[K_NN], float* qb, int& qn, 
     tie_out = (top == old && tie_out) || t34 == top;
 }
 
+// a node record's boxes (TreeView::rec): child 0 (or a bucket's own box) and child 1
+__device__ __forceinline__ float rec_dist0(float4 q, float4 r1, float4 r2)
+{
+    return box_dist2_rn(q.x, q.y, q.z, make_float4(r1.x, r1.y, r1.z, 0.f),
+                        make_float4(r1.w, r2.x, r2.y, 0.f));
+}
+__device__ __forceinline__ float rec_dist1(float4 q, float4 r2, float4 r3)
+{
+    return box_dist2_rn(q.x, q.y, q.z, make_float4(r2.z, r2.w, r3.x, 0.f),
+                        make_float4(r3.y, r3.z, r3.w, 0.f));
+}
+
 // squared distance from the query to a child (point for a leaf child)
 __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, const TreeView& t,
                                              int c, float4 q)
@@ -109,10 +121,15 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
         if (node < 0) {
             first = last = ~node;
         } else {
-            const int4 m = t.meta[node];
+            // the node's record in one round trip: meta and the child boxes (a
+            // leaf child's box is its point, so d equals the point's norm2)
+            const float4* rp = t.rec + 4 * (size_t)node;
+            const float4 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3];
+            const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
+                                     __float_as_int(r0.z), __float_as_int(r0.w));
             if (m.w - m.z + 1 > t.leaf) {
-                const float d0 = child_dist2(pos, t, m.x, xq);
-                const float d1 = child_dist2(pos, t, m.y, xq);
+                const float d0 = rec_dist0(xq, r1, r2);
+                const float d1 = rec_dist1(xq, r2, r3);
                 // a node whose distance equals a[32] can hold a tie: visit it
                 const bool v0 = __any_sync(FULL, d0 <= a[K_NN - 1]);
                 const bool v1 = __any_sync(FULL, d1 <= a[K_NN - 1]);
@@ -131,7 +148,7 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             first = m.z;
             last = m.w;
             // thresholds may have shrunk since the push: re-test the bucket
-            const float db = box_dist2_rn(xq.x, xq.y, xq.z, t.blo[node], t.bhi[node]);
+            const float db = rec_dist0(xq, r1, r2);
             if (!__any_sync(FULL, db <= a[K_NN - 1])) continue;
         }
         if (blist && lane == 0) {
@@ -357,10 +374,10 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
                 scan(~node, ~node);
                 continue;
             }
-            const float db = box_dist2_rn(xq.x, xq.y, xq.z, t.blo[node], t.bhi[node]);
-            if (!__any_sync(FULL, db <= T)) continue;
-            const int4 m = t.meta[node];
-            scan(m.z, m.w);
+            const float4* rp = t.rec + 4 * (size_t)node;
+            const float4 r0 = rp[0], r1 = rp[1], r2 = rp[2];
+            if (!__any_sync(FULL, rec_dist0(xq, r1, r2) <= T)) continue;
+            scan(__float_as_int(r0.z), __float_as_int(r0.w));
         }
         return;
     }

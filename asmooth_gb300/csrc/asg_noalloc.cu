@@ -11,7 +11,7 @@
 // device buffers for the inputs and outputs.
 //
 // Costs and limits of the fixed scratch:
-//   * the array (NOALLOC_BYTES, about 8 MB) is resident on every GPU that
+//   * the array (NOALLOC_BYTES, about 10 MB) is resident on every GPU that
 //     loads the library, until the process exits;
 //   * at most NOALLOC_MAX_N particles per call; larger inputs are rejected
 //     with ASG_ERR_NOALLOC_LIMIT;
@@ -35,7 +35,7 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 struct NoallocLayout {
     size_t pos_in, vel_in, igrp_in, rk_in, keys0, keys1, vals0, vals1, sort_tmp;
     size_t pos, vel, igrp, rk, t33, idx33, meta, parent, leaf_parent, flags;
-    size_t blo, bhi, dacc, dexp, err, total;
+    size_t blo, bhi, rec, dacc, dexp, err, total;
 };
 
 static constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -71,6 +71,7 @@ static NoallocLayout noalloc_layout(size_t n)
     L.flags = take(4 * m);
     L.blo = take(16 * m);
     L.bhi = take(16 * m);
+    L.rec = take(64 * m);
     L.dacc = take(8 * n);
     L.dexp = take(4 * n);
     L.err = take(16);
@@ -78,8 +79,8 @@ static NoallocLayout noalloc_layout(size_t n)
     return L;
 }
 
-// 224 bytes per particle plus the sort scratch, with room for alignment
-constexpr size_t NOALLOC_BYTES = 240u * (size_t)NOALLOC_MAX_N + 64u * 1024u;
+// 288 bytes per particle plus the sort scratch, with room for alignment
+constexpr size_t NOALLOC_BYTES = 304u * (size_t)NOALLOC_MAX_N + 64u * 1024u;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
@@ -173,12 +174,15 @@ extern "C" int asg_neighbor_search_noalloc(const float* d_x, int np, float left,
                       s);
     launch_tree_boxes(F4(L.pos), nullptr, np, LEAF_MAX, reinterpret_cast<int4*>(b + L.meta),
                       I(L.parent), I(L.flags), F4(L.blo), F4(L.bhi), s);
+    launch_tree_records(F4(L.pos), np, LEAF_MAX, reinterpret_cast<const int4*>(b + L.meta),
+                        F4(L.blo), F4(L.bhi), F4(L.rec), s);
     TreeView t;
     t.n = np;
     t.leaf = LEAF_MAX;
     t.meta = reinterpret_cast<const int4*>(b + L.meta);
     t.blo = F4(L.blo);
     t.bhi = F4(L.bhi);
+    t.rec = F4(L.rec);
     launch_knn_t33(F4(L.pos), t, F(L.t33), F(L.rk), I(L.idx33), nullptr, err, s);
     launch_knn_ties(F4(L.pos), t, F(L.t33), I(L.idx33), 0, err, s);
     launch_check_rk(F(L.rk), np, err, s);
