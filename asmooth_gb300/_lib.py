@@ -20,6 +20,8 @@ SIGNATURES = {
     "asg_strerror": (C.c_char_p, [_i]),
     "asg_last_error": (C.c_char_p, [_vp]),
     "asg_abi_version": (_i, []),
+    "asg_host_alloc": (_i, [C.c_size_t, C.POINTER(_vp)]),
+    "asg_host_free": (_i, [_vp]),
     "asg_neighbor_search": (_i, [_vp, _vp, _i, _f, _f]),
     "asg_assign_on_mesh": (_i, [_vp, _vp, _i, _f, _i, _i, _vp, _vp]),
     "asg_assign_on_meshes": (_i, [_vp, _vp, _i, _f, _vp, _i, _i, _i, _vp, _vp, _vp]),

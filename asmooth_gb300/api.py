@@ -66,6 +66,37 @@ def make_particles(x, v=None, dens=None, rk=None, igrp=None) -> np.ndarray:
     return p
 
 
+class _HostBlock:
+    """A block from asg_host_alloc, freed when the last array over it goes."""
+
+    def __init__(self, nbytes: int):
+        self._lib = _lib.load()
+        p = C.c_void_p()
+        rc = self._lib.asg_host_alloc(int(nbytes), C.byref(p))
+        if rc != 0 or not p.value:
+            raise MemoryError(f"asg_host_alloc({nbytes}): host memory could not be mapped "
+                              f"or pinned (status {rc}; pinning needs the CUDA driver)")
+        self.ptr = p.value
+        self.__array_interface__ = {"shape": (int(nbytes),), "typestr": "|u1",
+                                    "data": (self.ptr, False), "version": 3}
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            self._lib.asg_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+
+def host_array(shape, dtype=np.float32) -> np.ndarray:
+    """A zeroed C-contiguous array in huge-page pinned host memory
+    (asg_host_alloc): host<->device copies from and to it keep the link's
+    rate on multi-GB transfers.  Use it for the particle records and meshes
+    passed to ``Context.smooth`` and the other host-array calls."""
+    dtype = np.dtype(dtype)
+    shape = (shape,) if np.isscalar(shape) else tuple(shape)
+    n = int(np.prod(shape, dtype=np.int64)) * dtype.itemsize
+    return np.asarray(_HostBlock(max(n, 1)))[:n].view(dtype).reshape(shape)
+
+
 def make_halos(x, r, mass) -> np.ndarray:
     h = np.zeros(len(r), HALO_DTYPE)
     h["x"] = np.asarray(x, np.float32).reshape(-1, 3)

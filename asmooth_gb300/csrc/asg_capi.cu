@@ -4,13 +4,18 @@
 // largest particle set seen.  Each public call validates its arguments, queues
 // its kernels on the context stream, synchronises once at the end and turns
 // the device error word into a status code.
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <atomic>
 #include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/asmooth_gb300.h"
@@ -348,6 +353,71 @@ int ensure_rk_checked(asg_ctx* ctx)
 extern "C" {
 
 int asg_abi_version(void) { return ASG_ABI_VERSION; }
+
+}  // extern "C"
+
+// ---- huge-page pinned host blocks ------------------------------------------------
+namespace {
+std::mutex g_host_mu;
+std::unordered_map<void*, std::pair<void*, size_t>> g_host_blocks;  // block -> (mapping, length)
+
+size_t huge_page_bytes()
+{
+    size_t v = 0;
+    if (FILE* f = std::fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+        unsigned long long u = 0;
+        if (std::fscanf(f, "%llu", &u) == 1) v = (size_t)u;
+        std::fclose(f);
+    }
+    return (v >= (1u << 16) && v <= (1ull << 30) && (v & (v - 1)) == 0) ? v : (2u << 20);
+}
+}  // namespace
+
+extern "C" {
+
+int asg_host_alloc(size_t bytes, void** out)
+{
+    if (!out) return ASG_ERR_ARG;
+    *out = nullptr;
+    if (bytes == 0) return ASG_ERR_ARG;
+    const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+    const size_t huge = huge_page_bytes();
+    const bool use_huge = bytes >= huge;
+    const size_t align = use_huge ? huge : page;
+    const size_t len = (bytes + align - 1) / align * align;
+    const size_t map_len = use_huge ? len + align : len;
+    void* base = mmap(nullptr, map_len, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+    if (base == MAP_FAILED) return ASG_ERR_NOMEM;
+    char* p = reinterpret_cast<char*>(((uintptr_t)base + align - 1) / align * align);
+    if (use_huge) madvise(p, len, MADV_HUGEPAGE);  // advice only: base pages if refused
+    std::memset(p, 0, len);  // fault the pages in (as huge pages) before they are pinned
+    if (cudaHostRegister(p, len, cudaHostRegisterPortable) != cudaSuccess) {
+        cudaGetLastError();
+        munmap(base, map_len);
+        return ASG_ERR_NOMEM;
+    }
+    std::lock_guard<std::mutex> g(g_host_mu);
+    g_host_blocks[p] = {base, map_len};
+    *out = p;
+    return ASG_OK;
+}
+
+int asg_host_free(void* p)
+{
+    if (!p) return ASG_OK;
+    std::pair<void*, size_t> m;
+    {
+        std::lock_guard<std::mutex> g(g_host_mu);
+        auto it = g_host_blocks.find(p);
+        if (it == g_host_blocks.end()) return ASG_ERR_ARG;
+        m = it->second;
+        g_host_blocks.erase(it);
+    }
+    cudaHostUnregister(p);
+    cudaGetLastError();
+    munmap(m.first, m.second);
+    return ASG_OK;
+}
 
 const char* asg_strerror(int status)
 {

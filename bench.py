@@ -8,8 +8,9 @@ One step = index build (Morton sort + radix tree) + neighbour search + dens +
 deposit of all three meshes for one cube.  `value` times steps with inputs
 resident in HBM (CUDA events on the library's stream; L2 is flushed before
 every step and the inputs are larger than L2).  `e2e` times the public C-ABI
-call asg_smooth on pinned host Particle records, host<->device copies
-included (wall clock).  Under torchrun every rank runs an independent replica
+call asg_smooth on Particle records and meshes in the library's huge-page
+pinned host memory (asg_host_alloc), host<->device copies included (wall
+clock).  Under torchrun every rank runs an independent replica
 cube (the path does not exchange data); value = total particles / max time.
 
 --impl reference times the reference algorithm on the host cores instead.
@@ -282,11 +283,10 @@ def run_ours(args):
     d2h = rec_bytes + sum(4 * 6 * nc ** 3 for nc in ncs) + 16 * len(ncs)
     e2e = None
     if not args.no_e2e:
-        host = torch.empty(rec_bytes, dtype=torch.uint8, pin_memory=True)
-        p = host.numpy().view(api.PARTICLE_DTYPE)
+        # host arrays from the library's huge-page pinned allocator (asg_host_alloc)
+        p = api.host_array(n, api.PARTICLE_DTYPE)
         p[:] = api.make_particles(cube.x, cube.v)
-        mesh_host = [torch.empty(6 * nc ** 3, dtype=torch.float32, pin_memory=True).numpy()
-                     for nc in ncs]
+        mesh_host = [api.host_array(6 * nc ** 3) for nc in ncs]
         for _ in range(max(1, args.warmup)):
             ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
         e2e_times = []
@@ -383,17 +383,14 @@ def run_ours(args):
                  "h_rel_err_vs_fp32_positions": {"max": float(rel.max()),
                                                  "median": float(np.median(rel))}}
         if not args.no_e2e:
-            def pinned(shape, dt):
-                return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
-
-            cell_h = pinned(n, torch.int32)
+            cell_h = api.host_array(n, np.int32)
             cell_h[:] = cell
-            off_h = pinned((n, 3), torch.int16).view(np.uint16)
+            off_h = api.host_array((n, 3), np.uint16)
             off_h[:] = off
-            v_h = pinned((n, 3), torch.float32)
+            v_h = api.host_array((n, 3), np.float32)
             v_h[:] = cube.v
-            rk_o, dens_o = pinned(n, torch.float32), pinned(n, torch.float32)
-            mesh_q = [pinned(6 * nc ** 3, torch.float32) for nc in ncs]
+            rk_o, dens_o = api.host_array(n, np.float32), api.host_array(n, np.float32)
+            mesh_q = [api.host_array(6 * nc ** 3, np.float32) for nc in ncs]
 
             def call():
                 ctx.smooth_quantised(cell_h, off_h, v_h, cube.left, cube.right, 4.0, grid,

@@ -18,6 +18,7 @@
 #ifndef ASMOOTH_GB300_H
 #define ASMOOTH_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -63,6 +64,19 @@ const char* asg_strerror(int status);
 /* text of the last error seen by this context (CUDA message or argument check) */
 const char* asg_last_error(asg_ctx* ctx);
 int asg_abi_version(void);
+
+/* ---- host memory for particle and mesh arrays --------------------------------
+ * Page-locked host memory that the copies in asg_smooth and the other
+ * host-array calls read and write at the link's rate on every call.  Blocks of
+ * at least one transparent huge page are mapped on huge-page boundaries and
+ * advised as huge pages before CUDA pins them (registered portable, usable
+ * from every device); smaller blocks are pinned base pages.  On the Grace
+ * hosts of GB300 nodes (64 KB base pages) some multi-GB copies from ordinary
+ * pinned memory ran at 10-30 GB/s instead of about 200; the huge-page blocks
+ * did not.  *out is null on failure.  Free with asg_host_free (null is a
+ * no-op; a pointer this call did not return is ASG_ERR_ARG). */
+int asg_host_alloc(size_t bytes, void** out);
+int asg_host_free(void* p);
 
 /* ---- reference-shaped one-shot calls (host arrays) --------------------------- */
 

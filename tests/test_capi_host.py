@@ -51,6 +51,17 @@ def test_host_only_entry_points(lib):
     assert lib.asg_last_error(None) == b"no context"
 
 
+def test_host_alloc_argument_checks(lib):
+    import ctypes as C
+
+    assert lib.asg_host_alloc(16, None) == -1  # null out-pointer
+    out = C.c_void_p(1)
+    assert lib.asg_host_alloc(0, C.byref(out)) == -1 and not out.value  # zero bytes; out cleared
+    assert lib.asg_host_free(None) == 0  # null is a no-op
+    junk = C.create_string_buffer(64)
+    assert lib.asg_host_free(C.cast(junk, C.c_void_p)) == -1  # not a block of asg_host_alloc
+
+
 def test_particle_record_layout():
     from asmooth_gb300 import api
 

@@ -172,6 +172,23 @@ def test_fof_cube_vs_oracle(gpu_ctx, oracle):
     assert np.array_equal(po.canonical_groups(p["igrp"]), po.canonical_groups(lab))
 
 
+def test_smooth_on_huge_page_host_arrays(gpu_ctx):
+    """Records and meshes in asg_host_alloc blocks give the results of plain arrays."""
+    cube, ncs = syn.make_workload("cfg1", scale=2)
+    p1 = api.make_particles(cube.x, cube.v)
+    m1, t1, _, _ = gpu_ctx.smooth(p1, cube.left, cube.right, cube.boxsize, ncs, -1)
+    p2 = api.host_array(len(p1), api.PARTICLE_DTYPE)
+    p2[:] = api.make_particles(cube.x, cube.v)
+    m2 = [api.host_array(6 * nc ** 3) for nc in ncs]
+    _, t2, _, _ = gpu_ctx.smooth(p2, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=m2)
+    assert p1.tobytes() == p2.tobytes()
+    for a, b in zip(m1, m2):
+        assert np.array_equal(bits(a), bits(b))
+    assert np.array_equal(t1, t2)
+    big = api.host_array(600 * 2 ** 20, np.uint8)  # past one huge page on 64 KB-page hosts
+    assert big.nbytes == 600 * 2 ** 20 and big[::4096].sum() == 0
+
+
 def test_smooth_pipeline_matches_staged_calls(gpu_ctx):
     cube, ncs = syn.make_workload("cfg1", scale=2)
     rng = np.random.default_rng(5)
