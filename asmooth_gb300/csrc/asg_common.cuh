@@ -72,6 +72,20 @@ __device__ __forceinline__ float box_dist2_rn(float qx, float qy, float qz, floa
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
+// a tree node record's boxes (TreeView::rec words 1-3): child 0 (or a
+// bucket's own box) and child 1; a leaf child's box is its point, so the
+// distance equals norm2_rn to that point
+__device__ __forceinline__ float rec_dist0(float4 q, float4 r1, float4 r2)
+{
+    return box_dist2_rn(q.x, q.y, q.z, make_float4(r1.x, r1.y, r1.z, 0.f),
+                        make_float4(r1.w, r2.x, r2.y, 0.f));
+}
+__device__ __forceinline__ float rec_dist1(float4 q, float4 r2, float4 r3)
+{
+    return box_dist2_rn(q.x, q.y, q.z, make_float4(r2.z, r2.w, r3.x, 0.f),
+                        make_float4(r3.y, r3.z, r3.w, 0.f));
+}
+
 // double-float accumulation (Knuth two-sum): hi + lo carries ~48 bits
 // the same (hi, lo) as two_sum_acc for hi >= 0 and x >= 0: Fast2Sum on the
 // larger and the smaller operand gives the same rounded sum and the same exact

@@ -74,17 +74,22 @@ k_fof_link(const float4* __restrict__ pos, TreeView t, float ll2, int* P, int* e
         if (node < 0) {
             first = last = ~node;
         } else {
-            const int4 m = t.meta[node];
+            // the node's record: meta and both children's boxes in one round trip
+            const float4* rp = t.rec + 4 * (size_t)node;
+            const float4 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3];
+            const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
+                                     __float_as_int(r0.z), __float_as_int(r0.w));
             if (m.w - m.z + 1 > t.leaf) {
-                auto need = [&](int c) {
-                    // only partners with a larger sorted position are linked from q
-                    if (c < 0) return active && ~c > q;
-                    const int4 mc = t.meta[c];
-                    if (!(active && mc.w > q)) return false;
-                    return box_dist2_rn(xq.x, xq.y, xq.z, t.blo[c], t.bhi[c]) <= ll2;
-                };
-                const bool v0 = __any_sync(FM, need(m.x));
-                const bool v1 = __any_sync(FM, need(m.y));
+                // child 0 holds [m.z, g] and child 1 [g + 1, m.w]: the radix tree
+                // names its children by the split g (node or leaf g, and g + 1)
+                const int g = m.x >= 0 ? m.x : ~m.x;
+                // only partners with a larger sorted position are linked from q
+                const bool n0 = m.x < 0 ? (active && ~m.x > q)
+                                        : (active && g > q && rec_dist0(xq, r1, r2) <= ll2);
+                const bool n1 = m.y < 0 ? (active && ~m.y > q)
+                                        : (active && m.w > q && rec_dist1(xq, r2, r3) <= ll2);
+                const bool v0 = __any_sync(FM, n0);
+                const bool v1 = __any_sync(FM, n1);
                 if (sp + 2 > STACK_MAX) { overflow = true; break; }
                 if (lane == 0) {
                     if (v1) st[sp] = m.y;

@@ -53,18 +53,6 @@ __device__ __forceinline__ void knn_flush(float (&a)[K_NN], float* qb, int& qn, 
     tie_out = (top == old && tie_out) || t34 == top;
 }
 
-// a node record's boxes (TreeView::rec): child 0 (or a bucket's own box) and child 1
-__device__ __forceinline__ float rec_dist0(float4 q, float4 r1, float4 r2)
-{
-    return box_dist2_rn(q.x, q.y, q.z, make_float4(r1.x, r1.y, r1.z, 0.f),
-                        make_float4(r1.w, r2.x, r2.y, 0.f));
-}
-__device__ __forceinline__ float rec_dist1(float4 q, float4 r2, float4 r3)
-{
-    return box_dist2_rn(q.x, q.y, q.z, make_float4(r2.z, r2.w, r3.x, 0.f),
-                        make_float4(r3.y, r3.z, r3.w, 0.f));
-}
-
 // squared distance from the query to a child (point for a leaf child)
 __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, const TreeView& t,
                                              int c, float4 q)
