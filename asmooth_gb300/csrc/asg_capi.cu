@@ -382,7 +382,9 @@ int asg_host_alloc(size_t bytes, void** out)
     if (bytes == 0) return ASG_ERR_ARG;
     const size_t page = (size_t)sysconf(_SC_PAGESIZE);
     const size_t huge = huge_page_bytes();
-    const bool use_huge = bytes >= huge;
+    // from half a huge page up, whole huge pages (at most 2x the request):
+    // a block's pages must be huge for its copies to keep their rate
+    const bool use_huge = bytes >= huge / 2;
     const size_t align = use_huge ? huge : page;
     const size_t len = (bytes + align - 1) / align * align;
     const size_t map_len = use_huge ? len + align : len;

@@ -286,7 +286,11 @@ def run_ours(args):
         # host arrays from the library's huge-page pinned allocator (asg_host_alloc)
         p = api.host_array(n, api.PARTICLE_DTYPE)
         p[:] = api.make_particles(cube.x, cube.v)
-        mesh_host = [api.host_array(6 * nc ** 3) for nc in ncs]
+        mesh_block = api.host_array(sum(6 * nc ** 3 for nc in ncs))  # all meshes, one block
+        mesh_host, o = [], 0
+        for nc in ncs:
+            mesh_host.append(mesh_block[o:o + 6 * nc ** 3])
+            o += 6 * nc ** 3
         for _ in range(max(1, args.warmup)):
             ctx.smooth(p, cube.left, cube.right, cube.boxsize, ncs, -1, meshes=mesh_host)
         e2e_times = []
@@ -383,14 +387,22 @@ def run_ours(args):
                  "h_rel_err_vs_fp32_positions": {"max": float(rel.max()),
                                                  "median": float(np.median(rel))}}
         if not args.no_e2e:
-            cell_h = api.host_array(n, np.int32)
+            # inputs and outputs carved from one huge-page block
+            parts = [((n,), np.int32), ((n, 3), np.uint16), ((n, 3), np.float32),
+                     ((n,), np.float32), ((n,), np.float32)]
+            offs, o = [], 0
+            for shape, dt in parts:
+                offs.append(o)
+                o += -(-int(np.prod(shape)) * np.dtype(dt).itemsize // 256) * 256
+            qblock = api.host_array(o, np.uint8)
+            cell_h, off_h, v_h, rk_o, dens_o = [
+                qblock[a:a + int(np.prod(shape)) * np.dtype(dt).itemsize].view(dt).reshape(shape)
+                for (shape, dt), a in zip(parts, offs)]
             cell_h[:] = cell
-            off_h = api.host_array((n, 3), np.uint16)
             off_h[:] = off
-            v_h = api.host_array((n, 3), np.float32)
             v_h[:] = cube.v
-            rk_o, dens_o = api.host_array(n, np.float32), api.host_array(n, np.float32)
-            mesh_q = [api.host_array(6 * nc ** 3, np.float32) for nc in ncs]
+            mesh_q = [mesh_block[o - 6 * nc ** 3:o] for nc, o in
+                      zip(ncs, np.cumsum([6 * nc ** 3 for nc in ncs]))]
 
             def call():
                 ctx.smooth_quantised(cell_h, off_h, v_h, cube.left, cube.right, 4.0, grid,

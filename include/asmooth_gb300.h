@@ -68,13 +68,15 @@ int asg_abi_version(void);
 /* ---- host memory for particle and mesh arrays --------------------------------
  * Page-locked host memory that the copies in asg_smooth and the other
  * host-array calls read and write at the link's rate on every call.  Blocks of
- * at least one transparent huge page are mapped on huge-page boundaries and
- * advised as huge pages before CUDA pins them (registered portable, usable
- * from every device); smaller blocks are pinned base pages.  On the Grace
- * hosts of GB300 nodes (64 KB base pages) some multi-GB copies from ordinary
- * pinned memory ran at 10-30 GB/s instead of about 200; the huge-page blocks
- * did not.  *out is null on failure.  Free with asg_host_free (null is a
- * no-op; a pointer this call did not return is ASG_ERR_ARG). */
+ * at least half a transparent huge page are whole huge pages, mapped on
+ * huge-page boundaries and advised as huge pages before CUDA pins them
+ * (registered portable, usable from every device); smaller blocks are pinned
+ * base pages, so several small arrays are best carved from one block.  On the
+ * Grace hosts of GB300 nodes (64 KB base pages, 512 MB huge pages) some copies
+ * of hundreds of MB from ordinary pinned memory ran at 10-30 GB/s instead of
+ * about 200; from huge-page blocks they did not.  *out is null on failure.
+ * Free with asg_host_free (null is a no-op; a pointer this call did not
+ * return is ASG_ERR_ARG). */
 int asg_host_alloc(size_t bytes, void** out);
 int asg_host_free(void* p);
 
