@@ -252,15 +252,27 @@ k_mark_halos(const float4* __restrict__ pos, TreeView t, const float* __restrict
         if (node < 0) {
             first = last = ~node;
         } else {
-            const int4 m = t.meta[node];
-            if (box_dist2_rn(cx, cy, cz, t.blo[node], t.bhi[node]) >= r2) continue;
+            // the node's record: a node's children are tested by their boxes before
+            // they are pushed, a bucket (or a bucket root) by its own box
+            const float4* rp = t.rec + 4 * (size_t)node;
+            const float4 r0 = rp[0], r1 = rp[1], r2v = rp[2], r3 = rp[3];
+            const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
+                                     __float_as_int(r0.z), __float_as_int(r0.w));
+            const float4 c4 = make_float4(cx, cy, cz, 0.f);
             if (m.w - m.z + 1 > t.leaf) {
+                // a leaf child goes on as a one-particle bucket, tested by its norm2
+                const bool v0 = m.x < 0 || rec_dist0(c4, r1, r2v) < r2;
+                const bool v1 = m.y < 0 || rec_dist1(c4, r2v, r3) < r2;
                 if (sp + 2 > STACK_MAX) { overflow = true; break; }
-                if (lane == 0) { st[sp] = m.y; st[sp + 1] = m.x; }
-                sp += 2;
+                if (lane == 0) {
+                    if (v1) st[sp] = m.y;
+                    if (v0) st[sp + (v1 ? 1 : 0)] = m.x;
+                }
+                sp += (v0 ? 1 : 0) + (v1 ? 1 : 0);
                 __syncwarp();
                 continue;
             }
+            if (rec_dist0(c4, r1, r2v) >= r2) continue;
             first = m.z;
             last = m.w;
         }

@@ -216,10 +216,13 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
         if (node < 0) {
             first = last = ~node;
         } else {
-            const int4 m = t.meta[node];
+            const float4* rp = t.rec + 4 * (size_t)node;
+            const float4 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3];
+            const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
+                                     __float_as_int(r0.z), __float_as_int(r0.w));
             if (m.w - m.z + 1 > t.leaf) {
-                const bool v0 = __any_sync(FULL, child_dist2(pos, t, m.x, xq) <= T);
-                const bool v1 = __any_sync(FULL, child_dist2(pos, t, m.y, xq) <= T);
+                const bool v0 = __any_sync(FULL, rec_dist0(xq, r1, r2) <= T);
+                const bool v1 = __any_sync(FULL, rec_dist1(xq, r2, r3) <= T);
                 if (sp + 2 > STACK_MAX) { overflow = true; break; }
                 if (lane == 0) {
                     if (v1) st[sp] = m.y;
