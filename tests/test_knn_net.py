@@ -40,3 +40,21 @@ def test_flush_on_random_values():
         out = gen.run(merge, list(a) + vs, order)
         want = sorted(list(a) + list(v))
         assert out[:gen.KA + 1] == want[:gen.KA + 1]
+
+
+def test_queued_flush_model(tmp_path):
+    """The queue-and-merge top-33 (CPU model over the generated networks) gives
+    the exact 33rd distance and flags every exact tie."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        import pytest
+
+        pytest.skip("g++ not available")
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "knn_flush_model.cpp")
+    exe = str(tmp_path / "knn_flush_model")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", src, "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
