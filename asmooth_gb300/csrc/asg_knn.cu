@@ -8,9 +8,9 @@
 // smallest keys (the 33rd excluded, self included) receive the tent weight
 // ker(p, q, 1/rk) in dens.
 //
-// Three warp-bundle traversals of the radix tree; a warp serves the 32
-// consecutive (Morton-ordered) particles of one bundle, one lane per particle,
-// and visits a node when any lane needs it:
+// Three warp-bundle kernels over the radix tree (its 64-byte node records); a
+// warp serves the 32 consecutive (Morton-ordered) particles of one bundle, one
+// lane per particle, and visits a node when any lane needs it:
 //   k_knn_t33   per-lane sorted top-33 of d2 in registers, candidates queued
 //               and merged by comparator networks (asg_knn_net.cuh)
 //               -> t33 = 33rd smallest d2 (exact, with multiplicity)
@@ -20,6 +20,7 @@
 //               ker(q, j) to every j of its 32-set as 64-bit fixed point
 //               (per-receiver power-of-two scale, warp-aggregated integer
 //               atomics): exact integer sums, so deterministic in any order.
+//               It visits the buckets k_knn_t33 recorded for the bundle.
 #include <climits>
 
 #include "asg_common.cuh"
@@ -69,10 +70,12 @@ __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, con
 // 32-set is {d2 < t33} and needs no index), -2 when ties must be resolved.
 // Each lane keeps its 33 smallest d2 sorted in registers; a candidate with
 // d2 <= a[32] goes to the lane's queue in shared memory, and when any lane's
-// queue is full the warp merges every queue with two comparator networks
-// (sort the queue, odd-even merge with a[]), about a quarter of the min/max
-// work of inserting each candidate as it comes.  Thresholds are the merged
-// a[32], an upper bound of the true one while values wait in the queue.
+// queue holds more than KNN_QUEUE - 2 values after a step of two candidates
+// the warp merges every queue with two comparator networks (sort the queue,
+// odd-even merge with a[]), about a quarter of the min/max work of inserting
+// each candidate as it comes.  Thresholds are the merged a[32], an upper bound
+// of the true one while values wait in the queue.  The ids of the buckets
+// scanned go to blist for k_dens_scatter.
 __global__ void __launch_bounds__(KNN_WARPS * 32, 8)
 k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
           float* __restrict__ rk, int* __restrict__ idx33, int* __restrict__ blist, int* err)

@@ -302,7 +302,11 @@ def run_ours(args):
             e2e_times.append(time.perf_counter() - w0)
         tt = max_over_ranks(statistics.mean(e2e_times), dist)
         e2e = {"value": replica_value(n_local, world, tt), "unit": "particles/s",
-               "h2d_bytes_per_step": rec_bytes, "d2h_bytes_per_step": d2h}
+               "h2d_bytes_per_step": rec_bytes, "d2h_bytes_per_step": d2h,
+               # the spread of the calls behind the mean (host-link copy rates vary)
+               "call_ms": {"min": 1e3 * min(e2e_times),
+                           "median": 1e3 * statistics.median(e2e_times),
+                           "max": 1e3 * max(e2e_times)}}
         rk_host = p["rk"].copy()
     else:
         rk_d = torch.empty(n, dtype=torch.float32, device="cuda")
