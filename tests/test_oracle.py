@@ -182,3 +182,36 @@ def test_oracle_matches_reference_on_clustered_cube(oracle):
     rk_r, d_r = R.neighbor_search(cube.x, cube.left, cube.right)
     rk_o, d_o = oracle.neighbor_search(cube.x, cube.left, cube.right)
     assert np.array_equal(bits(rk_r), bits(rk_o)) and np.array_equal(bits(d_r), bits(d_o))
+
+
+@pytest.mark.skipif(not po.Reference.available(), reason="reference not built here")
+def test_oracle_matches_reference_on_cell_edges(oracle):
+    """Particles exactly on cell and 8-cell tile edges, with supports ending
+    exactly on edges, at the box faces and beyond them (clipping): the C
+    restatement of the three deposits equals the reference bit for bit."""
+    R = po.Reference()
+    L, nc = 64.0, 16  # cell 4 units, tile 32 units
+    rng = np.random.default_rng(11)
+    edges = np.arange(0, nc + 1, dtype=np.float32) * np.float32(L / nc)
+    x = rng.choice(edges, (400, 3)).astype(np.float32)
+    x[:100] += rng.choice([-1e-3, 0.0, 1e-3], (100, 3)).astype(np.float32)  # next to edges
+    x[100:120] = rng.uniform(-3, L + 3, (20, 3)).astype(np.float32)  # past the faces
+    rk = rng.choice(np.float32([2.0, 4.0, 6.0, 8.0, 3.999, 0.5]), 400).astype(np.float32)
+    v = rng.normal(size=(400, 3)).astype(np.float32)
+    dens = rng.uniform(0.5, 2.0, 400).astype(np.float32)
+    igrp = rng.choice([-1, 0, 2], 400).astype(np.int32)
+    for sign in (-1, 1):
+        m_o, _, _ = oracle.assign_on_mesh(x, v, dens, rk, igrp, L, nc, sign)
+        m_r = R.assign_on_mesh(x, v, dens, rk, igrp, L, nc, sign)
+        assert np.array_equal(bits(m_o), bits(m_r))
+        d_o = oracle.assign_on_density_mesh(x, rk, igrp, L, nc, sign)
+        d_r = R.assign_on_density_mesh(x, rk, igrp, L, nc, sign)
+        assert np.array_equal(bits(d_o), bits(d_r))
+        # the periodic variant (rank offset, wrapped cells) on particles inside [0, L)
+        inside = np.all((x >= 0) & (x < L), axis=1)
+        g_o, _, _ = oracle.assign_on_mesh(x[inside], v[inside], dens[inside], rk[inside],
+                                          igrp[inside], L, nc, sign, periodic=True,
+                                          offset=(L, 0.0, 2 * L))
+        g_r = R.assign_on_global_mesh(x[inside], v[inside], dens[inside], rk[inside],
+                                      igrp[inside], L, nc, sign, coords=(1, 0, 2))
+        assert np.array_equal(bits(g_o), bits(g_r))
