@@ -1,5 +1,5 @@
 // asg_index.cu -- the spatial index that replaces KDTreeSimple
-// (kdtree_balanced.cpp:251-350): particles are put in 48-bit Morton order by a
+// (kdtree_balanced.cpp:212-296): particles are put in 48-bit Morton order by a
 // stable LSD radix sort (each 8-bit digit pass is a counting sort: per-tile
 // digit histograms built with warp-aggregated shared-memory atomics, one
 // exclusive scan, a stable scatter), then a radix tree (Karras 2012) is built

@@ -11,15 +11,23 @@
 // device buffers for the inputs and outputs.
 //
 // Costs and limits of the fixed scratch:
-//   * the array (NOALLOC_BYTES, about 10 MB) is resident on every GPU that
-//     loads the library, until the process exits;
+//   * the array (NOALLOC_BYTES, about 10 MB) takes device memory on a GPU
+//     from the moment the library's module is loaded there until the process
+//     exits.  With CUDA's lazy module loading (the default) that is the first
+//     call into this file on that device, not the dlopen of the library, so a
+//     caller that reserves its memory pool up front makes a preparing call
+//     (np = 0 and null pointers) on each device before the reservation;
 //   * at most NOALLOC_MAX_N particles per call; larger inputs are rejected
 //     with ASG_ERR_NOALLOC_LIMIT;
 //   * every call on a device uses the same array and leaves the last call's
 //     contents in it, so calls that overlap on the GPU (other streams, other
 //     host threads) race and must be serialised by the caller;
-//   * the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress); make that first call before any stream capture.
+//   * the first call on each device (the preparing call, or the first search)
+//     looks up the array's device address (cudaGetSymbolAddress) and keeps it
+//     for later calls; make that first call before any stream capture.  After a
+//     cudaDeviceReset the kept address is stale: a preparing call looks it up
+//     again;
+//   * the call is synchronous: it returns when its work on the stream is done.
 #include <mutex>
 
 #include "../../include/asmooth_gb300.h"
@@ -79,7 +87,9 @@ static NoallocLayout noalloc_layout(size_t n)
     return L;
 }
 
-// 288 bytes per particle plus the sort scratch, with room for alignment
+// 248 bytes per particle in the arrays above plus the radix sort's scratch
+// (radix_sort_temp_bytes) and 256-byte alignment of every array: 304 bytes
+// per particle and 64 KB cover them (noalloc_layout checks the total)
 constexpr size_t NOALLOC_BYTES = 304u * (size_t)NOALLOC_MAX_N + 64u * 1024u;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
@@ -87,12 +97,13 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 static void* g_scratch_ptr[NOALLOC_MAX_DEVICES];
 static std::mutex g_scratch_mu;
 
-// device address of the scratch on the current device, looked up once per device
-static int scratch_address(int dev, void** out)
+// device address of the scratch on the current device, looked up once per
+// device (again when refresh is set: the preparing call)
+static int scratch_address(int dev, void** out, bool refresh)
 {
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return ASG_ERR_ARG;
     std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!g_scratch_ptr[dev] || refresh) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -134,6 +145,20 @@ using namespace asg;
 extern "C" int asg_neighbor_search_noalloc(const float* d_x, int np, float left, float right,
                                            float* d_rk, float* d_dens, void* stream)
 {
+    // an unread error of the caller's earlier CUDA work on this thread would be
+    // reported as this call's own: refuse before any work and leave it unread
+    if (cudaPeekAtLastError() != cudaSuccess) return ASG_ERR_CUDA;
+    if (np == 0 && !d_x && !d_rk && !d_dens) {
+        // preparing call: load the module on the current device (which places
+        // the scratch there) and look up the scratch's address
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) {
+            cudaGetLastError();
+            return ASG_ERR_CUDA;
+        }
+        void* base = nullptr;
+        return scratch_address(dev, &base, true);
+    }
     if (!d_x || !d_rk || !d_dens) return ASG_ERR_ARG;
     if (np < K_NN) return np > 0 ? ASG_ERR_FEW : ASG_ERR_ARG;
     if (np > NOALLOC_MAX_N) return ASG_ERR_NOALLOC_LIMIT;
@@ -146,7 +171,7 @@ extern "C" int asg_neighbor_search_noalloc(const float* d_x, int np, float left,
         return ASG_ERR_CUDA;
     }
     void* base = nullptr;
-    if (int r = scratch_address(dev, &base)) return r;
+    if (int r = scratch_address(dev, &base, false)) return r;
     unsigned char* b = static_cast<unsigned char*>(base);
     auto F4 = [&](size_t off) { return reinterpret_cast<float4*>(b + off); };
     auto F = [&](size_t off) { return reinterpret_cast<float*>(b + off); };

@@ -42,7 +42,6 @@ WORKLOADS = {
     "cfg5": ("cfg5", 1, "cfg5: 512^3 particles, side 1024, 20000 NFW halos, 8-unit periodic "
                         "shell, k=32, nc=128,256,512"),
 }
-CPU_SAMPLE = ("cfg2", 2)  # same model at 1/8 volume: 128^3 particles, side 256, nc = 32,64,128
 
 
 def env_int(k, d):
@@ -147,36 +146,36 @@ def deposit_cells(x, rk, boxsize, ncs, tile=8):
     return cells, tiles
 
 
-def cpu_reference_run(nthreads: int, use_ref: bool):
-    """One bounded sample of the workload on the host cores: tree + neighbour
-    search + deposit of the sample's meshes.  Returns (seconds, n_local, kind)."""
+def cpu_reference_run(nthreads: int, cube, ncs):
+    """One pass of the reference algorithm over `cube` on the host cores: the
+    C port of the reference's kd-tree construction, neighbour search (with its
+    dens scatter) and deposit of every mesh, OpenMP over nthreads cores, as the
+    reference's own OpenMP build runs them.  Returns seconds."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
-    from asmooth_gb300 import synthetic as syn
-
-    cube, ncs = syn.make_workload(CPU_SAMPLE[0], scale=CPU_SAMPLE[1])
     ig = np.zeros(cube.n, np.int32)
-    if use_ref and pyoracle.Reference.available(omp=True):
-        R = pyoracle.Reference(omp=True)
-        kind = "reference"
-        t0 = time.perf_counter()
-        rk, dens = R.neighbor_search(cube.x, cube.left, cube.right)  # serial kNN loop in the harness
-        for nc in ncs:
-            R.assign_on_mesh(cube.x, cube.v, dens, rk, ig, cube.boxsize, nc, -1)
-        dt = time.perf_counter() - t0
-        return dt, cube.n_local, kind, 1
     O = pyoracle.Oracle()
     t0 = time.perf_counter()
     rk, dens = O.neighbor_search(cube.x, cube.left, cube.right, nthreads=nthreads)
     for nc in ncs:
         O.assign_on_mesh(cube.x, cube.v, dens, rk, ig, cube.boxsize, nc, -1, nthreads=nthreads,
                          want64=False)
-    dt = time.perf_counter() - t0
-    return dt, cube.n_local, "port", nthreads
+    return time.perf_counter() - t0
+
+
+def workload_config(wl_desc: str, cube) -> dict:
+    """The `config` object of both arms' lines for one workload."""
+    return {"workload": wl_desc + ", plain FP32 form", "n_with_shell": int(cube.n),
+            "n_local": int(cube.n_local)}
 
 
 def run_reference(args):
+    """The reference algorithm on the host cores (the C port; the reference's
+    own build needs its sources, which the benchmark host does not have), on
+    the GPU arm's workload: every timed step is one full pass over the same
+    cube.  Warm-up steps run the same model at 1/8 volume (they only start the
+    threads and fault in the code), so the run stays within minutes."""
     rank = env_int("RANK", 0)
     if rank != 0:
         return 0
@@ -184,25 +183,28 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
+    from asmooth_gb300 import synthetic as syn
+
     pyoracle.build_oracle()
-    times = []
-    kind = "port"
-    n_local = 0
-    for k in range(args.warmup + args.steps):
-        dt, n_local, kind, cores = cpu_reference_run(nthreads, use_ref=False)
-        if k >= args.warmup:
-            times.append(dt)
+    gen, scale, wl_desc = WORKLOADS[args.workload]
+    cube, ncs = syn.make_workload(gen, seed=2, scale=scale)
+    small, sncs = syn.make_workload(gen, seed=2, scale=2 * scale)
+    for _ in range(args.warmup):
+        cpu_reference_run(nthreads, small, sncs)
+    times = [cpu_reference_run(nthreads, cube, ncs) for _ in range(args.steps)]
     sec = statistics.mean(times)
-    value = n_local / sec
-    sample = (f"{CPU_SAMPLE[0]} model at 1/8 volume: 128^3 particles, side 256, 8-unit shell, "
-              f"nc=32,64,128; tree + neighbour search + deposit per step")
+    value = cube.n_local / sec
+    sample = (f"the whole workload every timed step ({wl_desc}); C port of the reference's "
+              f"kd-tree + neighbour search + deposit, OpenMP over {nthreads} host cores; warm-up "
+              f"steps on the same model at 1/8 volume")
     line = {
         "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded NFW-clustered cube)", "impl": "reference",
-        "config": {"workload": f"{WORKLOAD} model, CPU sample: {sample}", "threads": nthreads},
-        "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nthreads, "kind": kind,
+        "data": "synthetic (seeded NFW-clustered cube in cubep3m layout)", "impl": "reference",
+        "config": workload_config(wl_desc, cube),
+        "threads": nthreads,
+        "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nthreads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -474,18 +476,18 @@ def run_ours(args):
 
         pyoracle.build_oracle()
         nthreads = os.cpu_count() or 1
-        dt, nl, kind, cores = cpu_reference_run(nthreads, use_ref=False)
-        cpu = {"value": nl / dt, "unit": "particles/s", "cores": cores, "kind": kind,
-               "sample": "cfg2 model at 1/8 volume (128^3 particles, side 256, nc=32,64,128), "
-                         "tree + neighbour search + deposit, OpenMP over all host cores"}
+        dt = cpu_reference_run(nthreads, cube, ncs)
+        cpu = {"value": n_local / dt, "unit": "particles/s", "cores": nthreads, "kind": "port",
+               "sample": f"one pass over the whole workload ({wl_desc}): C port of the "
+                         f"reference's kd-tree + neighbour search + deposit, OpenMP over "
+                         f"{nthreads} host cores"}
     line = {
         "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded NFW-clustered cube in cubep3m layout)",
-        "config": {"workload": wl_desc + ", plain FP32 form",
-                   "n_with_shell": n, "n_local": n_local, "parallelism": f"replicas x{world}",
-                   "l2": "flushed before every timed step; inputs larger than L2"},
+        "config": dict(workload_config(wl_desc, cube), parallelism=f"replicas x{world}",
+                       l2="flushed before every timed step; inputs larger than L2"),
         "e2e": e2e,
         "gpu_launches": launches,
         "roofline": roof,

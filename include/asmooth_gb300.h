@@ -347,14 +347,23 @@ int asg_deposit_stats(asg_ctx* ctx, long long* pairs, long long* tiles, long lon
  * Same results as asg_neighbor_search (rk = sqrtf of the 33rd neighbour d2,
  * tent weights added to dens), but inputs and outputs are the caller's device
  * arrays: d_x (np*3 floats), d_rk (np floats, written), d_dens (np floats,
- * added to).  The scratch is a fixed array inside the library, present on
- * every GPU that loads it until the process exits, so the call makes no
- * cudaMalloc/cudaFree.  Limits: 33 <= np <= ASG_NOALLOC_MAX_PARTICLES (larger
- * inputs return ASG_ERR_NOALLOC_LIMIT).  All calls on one device share that
- * scratch: calls that overlap on the GPU race, so serialise them.  The first
- * call on each device looks up the scratch's device address; make it before
- * any stream capture.  stream may be NULL (the default stream); the call
- * returns when the work on stream is complete. */
+ * added to).  The scratch is a fixed array inside the library (about 10 MB),
+ * so the call makes no cudaMalloc/cudaFree.  Limits: 33 <= np <=
+ * ASG_NOALLOC_MAX_PARTICLES (larger inputs return ASG_ERR_NOALLOC_LIMIT).
+ * All calls on one device share that scratch: calls that overlap on the GPU
+ * race, so serialise them.
+ * Preparing call: np = 0 with d_x, d_rk and d_dens all NULL loads the library's
+ * module on the current device, which is when the scratch takes its device
+ * memory (with CUDA's default lazy loading that is the first call on the
+ * device, not the loading of the library), looks up the scratch's device
+ * address and returns ASG_OK.  Make it on each device before reserving the
+ * memory pool, and again after a cudaDeviceReset (the address kept from before
+ * is stale then).  Without it the first search on a device does the same
+ * set-up; make that first call before any stream capture.
+ * stream may be NULL (the default stream).  The call is synchronous: it
+ * returns when its work on stream is complete.  It returns ASG_ERR_CUDA, before
+ * doing any work, when the calling thread holds an unread CUDA error from
+ * earlier work (left for the caller to read). */
 #define ASG_NOALLOC_MAX_PARTICLES 32768
 int asg_neighbor_search_noalloc(const float* d_x, int np, float left, float right, float* d_rk,
                                 float* d_dens, void* stream);

@@ -56,7 +56,7 @@ static inline double ker_integ64(double x1, double x2)
 }
 
 /* ------------------------------------------------------------------------- */
-/* KDTreeSimple (kdtree_balanced.cpp:251-350)                                 */
+/* KDTreeSimple (kdtree_balanced.cpp:212-296)                                 */
 /* ------------------------------------------------------------------------- */
 typedef struct {
     int direction;
@@ -119,7 +119,7 @@ static void free_tree(otree* t)
     memset(t, 0, sizeof(*t));
 }
 
-/* construct_tree_recursive (kdtree_balanced.cpp:284-350) in iterative form:
+/* construct_tree_recursive (kdtree_balanced.cpp:230-296) in iterative form:
  * bisect the node's box at the midpoint of the next axis with a Hoare
  * partition; same node numbering (pre-order, left subtree first) and the same
  * particle permutation; the parent's content[] is patched by index. */
@@ -464,6 +464,153 @@ int orc_dens_from_lists(const float* x, int n, const int* nbr, const float* t33,
 /* ------------------------------------------------------------------------- */
 /* mesh deposit                                                               */
 /* ------------------------------------------------------------------------- */
+
+/* One particle's deposit position and cell range: the plain form's clipped
+ * range (coarse_mesh.cpp:72-75) or the periodic form's shifted, unclipped one
+ * (global_mesh.cpp:52-69).  Returns 0 when the periodic form skips the
+ * particle (outside [0, boxsize)). */
+static int dep_range(const float* y, float h, float boxsize, int nc, int periodic,
+                     const float off[3], float xp[3], int lo[3], int hi[3])
+{
+    if (periodic) {
+        if (y[0] < 0.0f || y[0] >= boxsize || y[1] < 0.0f || y[1] >= boxsize ||
+            y[2] < 0.0f || y[2] >= boxsize)
+            return 0;
+        for (int i = 0; i < 3; ++i) xp[i] = y[i] + off[i];
+    } else {
+        for (int i = 0; i < 3; ++i) xp[i] = y[i];
+    }
+    for (int i = 0; i < 3; ++i) {
+        if (periodic) {
+            lo[i] = (int)floorf((xp[i] - h) / boxsize * nc);
+            hi[i] = 1 + (int)ceilf((xp[i] + h) / boxsize * nc);
+        } else {
+            int a = (int)((xp[i] - h) / boxsize * nc);
+            int b = 1 + (int)((xp[i] + h) / boxsize * nc);
+            lo[i] = a > 0 ? a : 0;
+            hi[i] = b < nc ? b : nc;
+        }
+    }
+    return 1;
+}
+
+/* The float and FP64 deposit of every particle, in parallel over the mesh's
+ * z-planes: each plane takes its particles in index order, so every cell sums
+ * its contributions in the serial loop's order and the float mesh is the
+ * serial one bit for bit.  The FP64 totals are summed per plane, then over
+ * the planes in order.  mesh64 holds the FP64 restatement (weights computed in
+ * double), or with fw the FP64 sums of the reference's float weights ker3,
+ * ker3*dens and ker3*v (products exact in double).  Returns -4 if some rk is
+ * not positive. */
+static int dep_by_planes(const float* x, const float* v, const float* dens, const float* rk,
+                         const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
+                         const float off[3], int nthreads, float* mesh, double* mesh64,
+                         double* totals, int fw)
+{
+    const size_t nmesh = (size_t)nc * nc * nc;
+    const float dx = boxsize / nc;
+    const int nc2 = nc * nc;
+    size_t* start = (size_t*)calloc((size_t)nc + 1, sizeof(size_t));
+    double* pt = (double*)calloc(2 * (size_t)nc, sizeof(double));
+    if (!start || !pt) { free(start); free(pt); return -2; }
+    int bad = 0;
+    /* entries (particle, z) per wrapped plane, particles in index order */
+    for (int j = 0; j < n; ++j) {
+        float xp[3]; int lo[3], hi[3];
+        const float h = rk[j];
+        if (!(h > 0.0f)) { bad = 1; continue; }
+        if (!dep_range(x + 3 * (size_t)j, h, boxsize, nc, periodic, off, xp, lo, hi)) continue;
+        for (int iz = lo[2]; iz < hi[2]; ++iz) start[((iz % nc) + nc) % nc + 1]++;
+    }
+    for (int p = 0; p < nc; ++p) start[p + 1] += start[p];
+    int* ej = (int*)malloc(start[nc] * sizeof(int) + 1);
+    int* ez = (int*)malloc(start[nc] * sizeof(int) + 1);
+    size_t* fill = (size_t*)malloc((size_t)nc * sizeof(size_t));
+    if (!ej || !ez || !fill) { free(ej); free(ez); free(fill); free(start); free(pt); return -2; }
+    memcpy(fill, start, (size_t)nc * sizeof(size_t));
+    for (int j = 0; j < n; ++j) {
+        float xp[3]; int lo[3], hi[3];
+        const float h = rk[j];
+        if (!(h > 0.0f)) continue;
+        if (!dep_range(x + 3 * (size_t)j, h, boxsize, nc, periodic, off, xp, lo, hi)) continue;
+        for (int iz = lo[2]; iz < hi[2]; ++iz) {
+            const size_t e = fill[((iz % nc) + nc) % nc]++;
+            ej[e] = j;
+            ez[e] = iz;
+        }
+    }
+    float* const mn = mesh;
+    float* const mh = mn + nmesh;
+    float* const mc = mh + nmesh;
+    float* const mv = mc + nmesh;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+    for (int p = 0; p < nc; ++p) {
+        double tn = 0.0, th = 0.0;
+        for (size_t e = start[p]; e < start[p + 1]; ++e) {
+            const int j = ej[e], iz = ez[e];
+            float xp[3]; int lo[3], hi[3];
+            const float h = rk[j];
+            dep_range(x + 3 * (size_t)j, h, boxsize, nc, periodic, off, xp, lo, hi);
+            const float hinv = 1.0f / h;
+            const float ds = dx * hinv;
+            const double hinv64 = 1.0 / (double)h;
+            const double ds64 = (double)dx * hinv64;
+            const int to_halo = sign * igrp[j] > 0;
+            float s1 = (iz * dx - xp[2]) * hinv;
+            const float k2 = ker_integ(s1, s1 + ds);
+            double t64 = ((double)iz * (double)dx - (double)xp[2]) * hinv64;
+            const double k2d = ker_integ64(t64, t64 + ds64);
+            for (int iy = lo[1]; iy < hi[1]; ++iy) {
+                s1 = (iy * dx - xp[1]) * hinv;
+                const float k1 = ker_integ(s1, s1 + ds);
+                t64 = ((double)iy * (double)dx - (double)xp[1]) * hinv64;
+                const double k1d = ker_integ64(t64, t64 + ds64);
+                for (int ix = lo[0]; ix < hi[0]; ++ix) {
+                    s1 = (ix * dx - xp[0]) * hinv;
+                    const float k0 = ker_integ(s1, s1 + ds);
+                    const size_t idx = (size_t)p * nc2 + (size_t)((iy % nc + nc) % nc) * nc +
+                                       (size_t)((ix % nc + nc) % nc);
+                    const float ker3 = k0 * k1 * k2;
+                    if (!to_halo) {
+                        mn[idx] += ker3;
+                        mc[idx] += ker3 * dens[j];
+                        mv[3 * idx] += ker3 * v[3 * (size_t)j];
+                        mv[3 * idx + 1] += ker3 * v[3 * (size_t)j + 1];
+                        mv[3 * idx + 2] += ker3 * v[3 * (size_t)j + 2];
+                        tn += (double)ker3;
+                    } else {
+                        mh[idx] += ker3;
+                        th += (double)ker3;
+                    }
+                    if (mesh64) {
+                        t64 = ((double)ix * (double)dx - (double)xp[0]) * hinv64;
+                        const double w = fw ? (double)ker3 : ker_integ64(t64, t64 + ds64) * k1d * k2d;
+                        if (!to_halo) {
+                            mesh64[idx] += w;
+                            mesh64[2 * nmesh + idx] += w * (double)dens[j];
+                            mesh64[3 * nmesh + 3 * idx] += w * (double)v[3 * (size_t)j];
+                            mesh64[3 * nmesh + 3 * idx + 1] += w * (double)v[3 * (size_t)j + 1];
+                            mesh64[3 * nmesh + 3 * idx + 2] += w * (double)v[3 * (size_t)j + 2];
+                        } else {
+                            mesh64[nmesh + idx] += w;
+                        }
+                    }
+                }
+            }
+        }
+        pt[2 * p] = tn;
+        pt[2 * p + 1] = th;
+    }
+    if (totals) {
+        totals[0] = totals[1] = 0.0;
+        for (int p = 0; p < nc; ++p) { totals[0] += pt[2 * p]; totals[1] += pt[2 * p + 1]; }
+    }
+    free(ej); free(ez); free(fill); free(start); free(pt);
+    return bad ? -4 : 0;
+}
+
 int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const float* rk,
                        const int* igrp, int n, float boxsize, int nc, int sign,
                        int periodic, const float* offset, int nthreads,
@@ -484,6 +631,12 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
     int bad = 0;
     if (nthreads < 1) nthreads = 1;
     const int par = nthreads > 1 && !mesh64 && !totals;
+    /* the FP64 sums in parallel, deterministically (the float mesh is the
+     * serial loop's); without them the loop below runs with the atomics of the
+     * reference's OpenMP build */
+    if (nthreads > 1 && (mesh64 || totals))
+        return dep_by_planes(x, v, dens, rk, igrp, n, boxsize, nc, sign, periodic, off, nthreads,
+                             mesh, mesh64, totals, 0);
 
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 64) num_threads(par ? nthreads : 1) reduction(| : bad)
@@ -601,6 +754,22 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
     }
     if (totals) { totals[0] = tot_n; totals[1] = tot_h; }
     return bad ? -4 : 0;
+}
+
+/* As orc_assign_on_mesh (float mesh the same bit for bit), with mesh64 the
+ * FP64 sums of the reference's float weights instead of the FP64 restatement:
+ * the value a deposit that sums those weights without rounding error gives. */
+int orc_assign_on_mesh_fw(const float* x, const float* v, const float* dens, const float* rk,
+                          const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
+                          const float* offset, int nthreads, float* mesh, double* mesh64,
+                          double* totals)
+{
+    if (!x || !v || !dens || !rk || !igrp || !mesh || !mesh64 || nc <= 0 || n < 0) return -1;
+    const float off[3] = {periodic && offset ? offset[0] : 0.0f,
+                          periodic && offset ? offset[1] : 0.0f,
+                          periodic && offset ? offset[2] : 0.0f};
+    return dep_by_planes(x, v, dens, rk, igrp, n, boxsize, nc, sign, periodic, off,
+                         nthreads < 1 ? 1 : nthreads, mesh, mesh64, totals, 1);
 }
 
 int orc_assign_on_density_mesh(const float* x, const float* rk, const int* igrp, int n,

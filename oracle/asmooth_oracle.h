@@ -27,7 +27,7 @@ extern "C" {
 
 #define ORC_K 33 /* KNeighbors::k (k_neighbors.h:47): 32 neighbours + self */
 
-/* Faithful neighbour search: KDTreeSimple::construct (kdtree_balanced.cpp:266-350)
+/* Faithful neighbour search: KDTreeSimple::construct (kdtree_balanced.cpp:212-296)
  * followed by neighbor_search for every particle in tree order
  * (clumping_tree_main.cpp:418-430, nbr_search.cpp:61-127).
  * rk[i]   <- sqrtf(d2 of the 33rd neighbour)            (input order)
@@ -66,6 +66,11 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
                        float* mesh, double* mesh64, double* totals);
 
 /* n-channel-only variant (coarse_mesh.cpp:212-269). mesh has nc^3 floats. */
+/* as orc_assign_on_mesh; mesh64 = FP64 sums of the reference's float weights */
+int orc_assign_on_mesh_fw(const float* x, const float* v, const float* dens, const float* rk,
+                          const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
+                          const float* offset, int nthreads, float* mesh, double* mesh64,
+                          double* totals);
 int orc_assign_on_density_mesh(const float* x, const float* rk, const int* igrp, int n,
                                float boxsize, int nc, int sign, float* mesh);
 

@@ -4,11 +4,15 @@
 # the single-rank MPI stand-in, into oracle/_ref/:
 #   libasmooth_ref.so      serial, -ffp-contract=off  (parity: bit-exact outputs)
 #   libasmooth_ref_omp.so  same with -fopenmp          (timing only)
-# Usage: oracle/build_ref.sh [reference_dir]   (default: $ASMOOTH_REFERENCE or /root/reference)
-# Exits 0 without building when the reference checkout is absent.
+# Usage: oracle/build_ref.sh <reference_dir>   (or $ASMOOTH_REFERENCE)
+# Exits 0 without building when no directory is given or it holds no reference.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${1:-${ASMOOTH_REFERENCE:-/root/reference}}
+REF=${1:-${ASMOOTH_REFERENCE:-}}
+if [ -z "$REF" ]; then
+    echo "build_ref: no reference directory given (argument or ASMOOTH_REFERENCE); nothing built"
+    exit 0
+fi
 if [ ! -f "$REF/nbr_search.cpp" ]; then
     echo "build_ref: reference sources not found at $REF; nothing built"
     exit 0

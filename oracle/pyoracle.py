@@ -35,9 +35,11 @@ def build_oracle(force: bool = False) -> str:
     return ORC_SO
 
 
-def build_reference() -> bool:
-    """Compile the reference harness from the reference checkout when present."""
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
+def build_reference(ref_dir: str | None = None) -> bool:
+    """Compile the reference harness from the reference checkout in ref_dir (or
+    $ASMOOTH_REFERENCE) when it is present; True when the harness exists."""
+    ref_dir = ref_dir or os.environ.get("ASMOOTH_REFERENCE", "")
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), ref_dir])
     return os.path.exists(os.path.join(REF_DIR, "libasmooth_ref.so"))
 
 
@@ -51,7 +53,8 @@ class Oracle:
         self.lib = C.CDLL(ORC_SO)
         L = self.lib
         for name in ("orc_neighbor_search", "orc_knn_exact", "orc_dens_from_lists",
-                     "orc_assign_on_mesh", "orc_assign_on_density_mesh", "orc_normalise_mesh",
+                     "orc_assign_on_mesh", "orc_assign_on_mesh_fw", "orc_assign_on_density_mesh",
+                     "orc_normalise_mesh",
                      "orc_group_fof", "orc_remove_small_groups", "orc_mark_halo_particles",
                      "orc_fof_halos", "orc_decode_zip"):
             getattr(L, name).restype = C.c_int
@@ -98,14 +101,18 @@ class Oracle:
 
     # -- mesh ----------------------------------------------------------------
     def assign_on_mesh(self, x, v, dens, rk, igrp, boxsize, nc, sign=-1, periodic=False,
-                       offset=(0.0, 0.0, 0.0), nthreads=1, want64=True):
+                       offset=(0.0, 0.0, 0.0), nthreads=1, want64=True, float_weights=False):
+        """(float mesh, FP64 mesh, FP64 totals).  The FP64 mesh is the FP64
+        restatement, or with float_weights the FP64 sums of the reference's
+        float weights (ker3, ker3*dens, ker3*v)."""
         x = np.ascontiguousarray(x, np.float32)
         n = x.shape[0]
         mesh = np.zeros(6 * nc ** 3, np.float32)
         m64 = np.zeros(6 * nc ** 3, np.float64) if want64 else None
         tot = np.zeros(2, np.float64) if want64 else None
         off = np.asarray(offset, np.float32)
-        rc = self.lib.orc_assign_on_mesh(
+        fn = self.lib.orc_assign_on_mesh_fw if float_weights else self.lib.orc_assign_on_mesh
+        rc = fn(
             _p(x), _p(np.ascontiguousarray(v, np.float32)), _p(np.ascontiguousarray(dens, np.float32)),
             _p(np.ascontiguousarray(rk, np.float32)), _p(np.ascontiguousarray(igrp, np.int32)),
             C.c_int(n), C.c_float(boxsize), C.c_int(nc), C.c_int(sign), C.c_int(int(periodic)),

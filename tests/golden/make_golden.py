@@ -2,7 +2,9 @@
 
 Runs the reference's own hot-path functions (compiled from the reference
 sources into oracle/_ref by oracle/build_ref.sh; serial, -ffp-contract=off) on
-two small seeded node-cubes and stores inputs and outputs as compressed npz:
+two small seeded node-cubes and stores inputs and outputs as compressed npz.
+Usage: python tests/golden/make_golden.py <reference checkout, e.g. /root/reference>
+
 
   plummer_s4.npz  Plummer-sphere cube (side 32, 16^3 particles + 8-unit shell)
   nfw_s16.npz     NFW-halo cube       (side 32, 16^3 particles + 8-unit shell)
@@ -77,7 +79,8 @@ def make(name: str, cube: syn.Cube, ncs, seed: int) -> None:
 
 
 def main():
-    if not po.build_reference():
+    # the reference checkout: first argument or $ASMOOTH_REFERENCE
+    if not po.build_reference(sys.argv[1] if len(sys.argv) > 1 else None):
         sys.exit("reference sources not available: cannot regenerate golden fixtures")
     cube, ncs = syn.make_workload("cfg1", scale=4)
     make("plummer_s4.npz", cube, ncs, 11)

@@ -1,0 +1,135 @@
+"""GPU deposit on adversarial inputs: particles exactly on cell and 8-cell tile
+edges and next to them, supports that end exactly on edges, particles past the
+box faces (clipping), halo and non-halo particles under both signs, in the
+plain (coarse_mesh.cpp:45-127), periodic (global_mesh.cpp:25-123) and
+density-only (coarse_mesh.cpp:212-269) deposits.
+
+Two checks, both through the C ABI:
+  * disjoint supports: the particles are split into batches whose cell boxes
+    do not overlap, so every cell receives at most one weight; then every
+    channel equals the reference's float mesh (the oracle restatement, pinned
+    bit for bit to the reference on these inputs on the CPU) bit for bit: each
+    per-cell weight ker3 = (k0*k1)*k2 and each product with dens and v is the
+    reference's float value;
+  * the whole set at once: n, c and halo are the correctly rounded FP64 sums of
+    the reference's float weights (error at most 2^-24 relative plus the
+    double-float accumulation's 2^-38), v within 1e-5 of |v| + n, and the FP64
+    mass totals within 1e-12 of the FP64 sums of the float weights."""
+import numpy as np
+import pytest
+
+from asmooth_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+L = 64.0
+NCS = (16, 32)  # cells of 4 and 2 units; 8-cell tiles of 32 and 16 units
+ROUND_TOL = 2.0 ** -24 + 2.0 ** -38
+V_TOL = 1e-5
+TOTAL_TOL = 1e-12
+
+
+def bits(a):
+    return np.asarray(a, np.float32).view(np.int32)
+
+
+def edge_inputs(seed=11, n=400):
+    rng = np.random.default_rng(seed)
+    edges = np.arange(0, 33, dtype=np.float32) * np.float32(2.0)  # every cell edge of nc = 32
+    x = rng.choice(edges, (n, 3)).astype(np.float32)
+    x[:100] += rng.choice([-1e-3, 0.0, 1e-3], (100, 3)).astype(np.float32)  # next to edges
+    x[100:120] = rng.uniform(-3, L + 3, (20, 3)).astype(np.float32)  # past the faces
+    rk = rng.choice(np.float32([2.0, 4.0, 6.0, 8.0, 3.999, 0.5, 1.0]), n).astype(np.float32)
+    v = rng.normal(size=(n, 3)).astype(np.float32)
+    dens = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    igrp = rng.choice([-1, 0, 2], n).astype(np.int32)
+    return x, v, dens, rk, igrp
+
+
+def axis_cells(x, h, nc, periodic):
+    """A superset of the cells each particle touches along one axis, as a
+    boolean (n, nc) array (one cell of margin on each side; wrapped when periodic)."""
+    f = (x.astype(np.float64) / L) * nc
+    w = (h.astype(np.float64) / L) * nc
+    lo = np.floor(f - w).astype(np.int64) - 1
+    hi = np.floor(f + w).astype(np.int64) + 2
+    cells = np.zeros((x.size, nc), bool)
+    for i in range(x.size):
+        r = np.arange(lo[i], hi[i])
+        r = np.mod(r, nc) if periodic else r[(r >= 0) & (r < nc)]
+        cells[i, r] = True
+    return cells
+
+
+def disjoint_batches(x, rk, nc, periodic):
+    """Greedy split into batches whose particles' cell boxes do not overlap."""
+    ax = [axis_cells(x[:, a], rk, nc, periodic) for a in range(3)]
+    batches = []
+    for i in range(x.shape[0]):
+        for b in batches:
+            clash = np.ones(len(b), bool)
+            for a in range(3):
+                clash &= (ax[a][b] & ax[a][i]).any(axis=1)
+            if not clash.any():
+                b.append(i)
+                break
+        else:
+            batches.append([i])
+    return batches
+
+
+def gpu_mesh(ctx, mode, x, v, dens, rk, igrp, nc, sign):
+    p = api.make_particles(x, v, dens=dens, rk=rk, igrp=igrp)
+    if mode == "plain":
+        m, t = ctx.assign_on_meshes(p, L, [nc], sign)
+        return m[0], t[0]
+    if mode == "periodic":
+        return ctx.assign_on_global_mesh(p, L, nc, sign, coords=(1, 0, 2))
+    return ctx.assign_on_density_mesh(p, L, nc, sign), None
+
+
+def oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign):
+    """(float mesh, FP64 sums of the float weights, FP64 totals) in the GPU
+    call's layout (density-only: the n channel)."""
+    per = mode == "periodic"
+    m, m64, t64 = oracle.assign_on_mesh(x, v, dens, rk, igrp, L, nc, sign, periodic=per,
+                                        offset=(L, 0.0, 2 * L), float_weights=True)
+    if mode == "density":
+        d = oracle.assign_on_density_mesh(x, rk, igrp, L, nc, sign)
+        assert np.array_equal(bits(d), bits(m[: nc ** 3]))  # the n channel of the plain deposit
+        return d, m64[: nc ** 3], t64
+    return m, m64, t64
+
+
+@pytest.mark.parametrize("mode", ["plain", "periodic", "density"])
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("nc", NCS)
+def test_deposit_edges(gpu_ctx, oracle, mode, sign, nc):
+    x, v, dens, rk, igrp = edge_inputs()
+    if mode == "periodic":  # the periodic deposit takes the particles inside [0, L)
+        inside = np.all((x >= 0) & (x < L), axis=1)
+        x, v, dens, rk, igrp = x[inside], v[inside], dens[inside], rk[inside], igrp[inside]
+    nm = nc ** 3
+
+    # one weight per cell: bit for bit the reference's float mesh
+    batches = disjoint_batches(x, rk, nc, mode == "periodic")
+    assert len(batches) < len(x)  # the batches do combine particles
+    for b in batches:
+        b = np.asarray(b)
+        got, _ = gpu_mesh(gpu_ctx, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
+        ref, _, _ = oracle_mesh(oracle, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
+        assert np.array_equal(bits(got), bits(ref)), (mode, sign, nc, b[:4])
+
+    # the whole set: correctly rounded FP64 sums of the float weights
+    got, tot = gpu_mesh(gpu_ctx, mode, x, v, dens, rk, igrp, nc, sign)
+    _, s64, t64 = oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign)
+    chans = [(0, nm)] if mode == "density" else [(0, nm), (nm, 2 * nm), (2 * nm, 3 * nm)]
+    for a, e in chans:
+        g, s = got[a:e].astype(np.float64), s64[a:e]
+        assert np.all(np.abs(g - s) <= ROUND_TOL * np.abs(s) + 1e-300), (mode, sign, nc, a)
+    if mode != "density":
+        vs = s64[3 * nm:]
+        scale = np.abs(vs) + np.repeat(s64[:nm], 3)
+        assert np.all(np.abs(got[3 * nm:].astype(np.float64) - vs) <= V_TOL * scale + 1e-30)
+        for k in range(2):
+            assert abs(tot[k] - t64[k]) <= TOTAL_TOL * max(abs(t64[k]), 1e-300), (k, tot, t64)

@@ -5,9 +5,11 @@ owns the whole GPU and lends libraries only its own buffers).
 It is called through the C ABI on the caller's device buffers, twice in a row
 (the fixed scratch keeps the first call's contents), and must give the same rk
 and dens as the allocating neighbour search on the same particles: rk bit for
-bit, dens within the 1e-5 relative tolerance of the other parity tests.  This
-file is collected last so that a run stopping at the first failure has
-already run every other test."""
+bit, dens within the 1e-5 relative tolerance of the other parity tests.  The
+second call adds onto a non-zero dens, as the reference's `dens +=` does, and
+must leave the device's free memory unchanged.  This file is collected last
+so that a run stopping at the first failure has already run every other
+test."""
 import ctypes as C
 
 import numpy as np
@@ -41,17 +43,29 @@ def test_noalloc_matches_allocating_search():
     torch.cuda.synchronize()
     rk_ref, dens_ref = rk_ref.cpu().numpy(), dens_ref.cpu().numpy()
 
-    for _ in range(2):  # the second call runs on the scratch the first one left behind
-        rk = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
-        dens = torch.zeros(n, dtype=torch.float32, device="cuda")
+    # preparing call: loads the module (places the scratch) and finds its address
+    assert lib.asg_neighbor_search_noalloc(None, 0, 0.0, 0.0, None, None, None) == 0
+
+    # every buffer of both calls exists before the first one runs
+    dens0 = np.random.default_rng(3).uniform(0.5, 2.0, n).astype(np.float32)
+    bufs = [(torch.full((n,), -1.0, dtype=torch.float32, device="cuda"),
+             torch.from_numpy(d).cuda()) for d in (np.zeros(n, np.float32), dens0)]
+    torch.cuda.synchronize()
+    free = []
+    for (rk, dens), d_in in zip(bufs, (np.zeros(n, np.float32), dens0)):
+        # the second call runs on the scratch the first one left behind
         rc = lib.asg_neighbor_search_noalloc(C.c_void_p(x_d.data_ptr()), n, cube.left, cube.right,
                                              C.c_void_p(rk.data_ptr()), C.c_void_p(dens.data_ptr()),
                                              None)
         assert rc == 0, lib.asg_strerror(rc)
         torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info()[0])
         rk_h, dens_h = rk.cpu().numpy(), dens.cpu().numpy()
         assert np.array_equal(rk_h.view(np.int32), rk_ref.view(np.int32))
-        assert np.max(np.abs(dens_h - dens_ref) / dens_ref) <= FIELD_TOL
+        want = d_in.astype(np.float64) + dens_ref  # dens is added to, not overwritten
+        assert np.max(np.abs(dens_h - want) / want) <= FIELD_TOL
+    # the call allocated nothing on the device
+    assert free[1] == free[0]
 
     # inputs beyond the fixed scratch are refused with a clear status
     big = torch.zeros((32769, 3), dtype=torch.float32, device="cuda")
