@@ -314,7 +314,7 @@ void load_quant_device(asg_ctx* ctx, const int* d_cell, const uint16_t* d_off, c
     launch_unpack_quant(d_cell, d_off, d_v, np, grid, left, cell_size, P<float4>(ctx->pos_in),
                         P<float4>(ctx->vel_in), P<int>(ctx->igrp_in), P<float>(ctx->rk_in),
                         ctx->d_err, ctx->s);
-    launch_morton(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
+    launch_space_keys(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
                   P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
 }
@@ -607,7 +607,7 @@ static int load_shell(asg_ctx* ctx, int np, float boxsize, float bf, int* np_wit
     ctx->left = -dx;
     ctx->right = boxsize + dx;
     phase_begin(ctx, ASG_PH_INDEX);
-    launch_morton(P<float4>(ctx->pos_in), n, ctx->left, ctx->right, nullptr, 0,
+    launch_space_keys(P<float4>(ctx->pos_in), n, ctx->left, ctx->right, nullptr, 0,
                   P<uint64_t>(ctx->keys0), P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
     int r = finish(ctx, "load_periodic_cube");
@@ -632,7 +632,7 @@ int asg_load_particles(asg_ctx* ctx, const asg_particle* p, int np, float left, 
     phase_begin(ctx, ASG_PH_INDEX);
     launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
                       P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
-    launch_morton(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
+    launch_space_keys(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
                   P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
     int r = finish(ctx, "load");
@@ -654,7 +654,7 @@ int asg_load_particles_device(asg_ctx* ctx, const float* d_x, const float* d_v,
     phase_begin(ctx, ASG_PH_INDEX);
     launch_unpack_soa(d_x, d_v, d_dens, d_igrp, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
                       P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
-    launch_morton(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
+    launch_space_keys(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
                   P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
     int r = finish(ctx, "load_device");
@@ -1252,7 +1252,7 @@ static int load_for_deposit(asg_ctx* ctx, const asg_particle* p, int np)
     phase_begin(ctx, ASG_PH_INDEX);
     launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
                       P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
-    launch_morton(P<float4>(ctx->pos_in), np, 0.0f, 0.0f, P<int>(ctx->lohi), 0,
+    launch_space_keys(P<float4>(ctx->pos_in), np, 0.0f, 0.0f, P<int>(ctx->lohi), 0,
                   P<uint64_t>(ctx->keys0), P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
     int r = finish(ctx, "load");
@@ -1508,7 +1508,7 @@ int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, f
     phase_begin(ctx, ASG_PH_INDEX);
     launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
                       P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
-    launch_morton(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
+    launch_space_keys(P<float4>(ctx->pos_in), np, left, right, nullptr, 0, P<uint64_t>(ctx->keys0),
                   P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
     run_knn(ctx);
@@ -1625,7 +1625,7 @@ int batch_queue_item(asg_batch* b, asg_ctx* ctx, int i, uint32_t cap)
     launch_unpack_soa(P<float>(b->in_x) + 3 * o, P<float>(b->in_v) + 3 * o, nullptr, nullptr, n,
                       P<float4>(ctx->pos_in), P<float4>(ctx->vel_in), P<int>(ctx->igrp_in),
                       P<float>(ctx->rk_in), ctx->d_err, ctx->s);
-    launch_morton(P<float4>(ctx->pos_in), n, ctx->left, ctx->right, nullptr, 0,
+    launch_space_keys(P<float4>(ctx->pos_in), n, ctx->left, ctx->right, nullptr, 0,
                   P<uint64_t>(ctx->keys0), P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
     run_knn(ctx);

@@ -15,13 +15,13 @@ namespace asg {
 constexpr int K_NN = 33;        // KNeighbors::k (k_neighbors.h:47): 32 neighbours + self
 constexpr int LEAF_MAX = 32;    // largest bucket: a tree node with <= leaf particles (leaf <= 32) is scanned whole
 constexpr int STACK_MAX = 128;  // traversal stack entries per warp
-constexpr int TIE_MAX = 16;     // exact d2 ties tracked at the 33rd neighbour
+constexpr int TIE_MAX = 16;     // exact d2 ties kept per pass of k_knn_ties at the 33rd neighbour
 
 // device error bits (ctx->d_err)
 constexpr int ERR_STACK = 1;       // traversal stack overflow
 constexpr int ERR_FEW = 2;         // a query found fewer than 33 particles
 constexpr int ERR_ZERO_RK = 4;     // 33rd distance is zero (>= 33 coincident particles)
-constexpr int ERR_TIES = 8;        // more than TIE_MAX exact ties at the 33rd neighbour
+constexpr int ERR_TIES = 8;        // tie selection ran out of passes (not reached for k = 33)
 constexpr int ERR_NONFINITE = 16;  // NaN / inf position
 constexpr int ERR_UF = 32;         // union-find retry limit hit
 constexpr int ERR_RANGE = 64;      // periodic deposit range wider than the mesh
@@ -49,17 +49,35 @@ __device__ __forceinline__ float ker_rn(float ax, float ay, float az, float bx, 
     return w;
 }
 
-// f, ker_integ (coarse_mesh.cpp:10-22): exact cell integral of the unit tent
-__device__ __forceinline__ float tent_f_rn(float x)
+// The integral of the unit tent max(0, 1 - |t|) over [a, b] (a < b), the cell
+// weight of f/ker_integ (coarse_mesh.cpp:10-22), evaluated without
+// cancellation.  The reference forms F(b) - F(a) with F(t) = t - t^2/2 (t < 1),
+// which cancels when a support ends a sliver inside a cell (0.5 - F(a) for a
+// just below 1); here each case uses its factored form, e.g. (1 - a)^2 / 2.
+// Every operation is explicitly rounded, so the C restatement in the oracle
+// gives the same bits.
+__device__ __forceinline__ float tent_pos_rn(float t)  // F(t) for t >= 0
 {
-    return x >= 1.0f ? 0.5f : __fsub_rn(x, __fmul_rn(__fmul_rn(0.5f, x), x));
+    return t >= 1.0f ? 0.5f : __fmul_rn(t, __fsub_rn(1.0f, __fmul_rn(0.5f, t)));
 }
-__device__ __forceinline__ float ker_integ_rn(float x1, float x2)
+__device__ __forceinline__ float tent_integral_rn(float a, float b)
 {
-    const float fac1 = x1 > 0.0f ? 1.0f : -1.0f;
-    const float fac2 = x2 > 0.0f ? 1.0f : -1.0f;
-    return __fsub_rn(__fmul_rn(fac2, tent_f_rn(__fmul_rn(fac2, x2))),
-                     __fmul_rn(fac1, tent_f_rn(__fmul_rn(fac1, x1))));
+    if (a >= 1.0f || b <= -1.0f) return 0.0f;
+    if (a >= 0.0f) {  // 0 <= a < 1
+        if (b >= 1.0f) {
+            const float u = __fsub_rn(1.0f, a);
+            return __fmul_rn(__fmul_rn(0.5f, u), u);
+        }
+        return __fmul_rn(__fsub_rn(b, a), __fsub_rn(1.0f, __fmul_rn(0.5f, __fadd_rn(a, b))));
+    }
+    if (b <= 0.0f) {  // a < b <= 0
+        if (a <= -1.0f) {
+            const float u = __fadd_rn(1.0f, b);
+            return __fmul_rn(__fmul_rn(0.5f, u), u);
+        }
+        return __fmul_rn(__fsub_rn(b, a), __fadd_rn(1.0f, __fmul_rn(0.5f, __fadd_rn(a, b))));
+    }
+    return __fadd_rn(tent_pos_rn(b), tent_pos_rn(-a));  // a < 0 < b
 }
 
 // squared distance from a point to an AABB, rounded so that for every point p
@@ -70,6 +88,46 @@ __device__ __forceinline__ float box_dist2_rn(float qx, float qy, float qz, floa
     const float dy = fmaxf(fmaxf(__fsub_rn(lo.y, qy), __fsub_rn(qy, hi.y)), 0.0f);
     const float dz = fmaxf(fmaxf(__fsub_rn(lo.z, qz), __fsub_rn(qz, hi.z)), 0.0f);
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// ---- pruning-only box test --------------------------------------------------
+// max of three floats (PTX three-input max, sm_100 and later)
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Squared distance from a point to an AABB in the cheaper FMA form, for
+// pruning only: compare it against prune_bound(t), never against t itself.
+// Per axis d = fl(lo - q) (or fl(q - hi)) is at most |fl(p - q)| for every
+// point p of the box (rounding is monotone); the FMA sum is at most
+// (dx^2 + dy^2 + dz^2)(1 + u)^3 and norm2_rn(q, p) is at least
+// (px^2 + py^2 + pz^2)(1 - u)^3 (u = 2^-24), so the result is at most
+// norm2_rn(q, p)(1 + 6.1u) for every p in the box.
+__device__ __forceinline__ float box_dist2_fast(float qx, float qy, float qz, float lx, float ly,
+                                                float lz, float hx, float hy, float hz)
+{
+    const float dx = max3f(lx - qx, qx - hx, 0.0f);
+    const float dy = max3f(ly - qy, qy - hy, 0.0f);
+    const float dz = max3f(lz - qz, qz - hz, 0.0f);
+    return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+}
+
+// the bound that box_dist2_fast is compared against for a threshold t on
+// norm2_rn: fl(t (1 + 2^-21)) >= t (1 + 6.9u) > t (1 + 6.1u), so a box holding
+// a point with norm2_rn <= t is never pruned (t = +inf stays +inf)
+__device__ __forceinline__ float prune_bound(float t) { return __fmul_rn(t, 1.0f + 0x1p-21f); }
+
+// the record boxes in the fast form (see rec_dist0 / rec_dist1 below)
+__device__ __forceinline__ float rec_fast0(float4 q, float4 r1, float4 r2)
+{
+    return box_dist2_fast(q.x, q.y, q.z, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y);
+}
+__device__ __forceinline__ float rec_fast1(float4 q, float4 r2, float4 r3)
+{
+    return box_dist2_fast(q.x, q.y, q.z, r2.z, r2.w, r3.x, r3.y, r3.z, r3.w);
 }
 
 // a tree node record's boxes (TreeView::rec words 1-3): child 0 (or a
@@ -110,7 +168,7 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x)
 
 // ---- Morton keys ------------------------------------------------------------
 // spread the low 21 bits of v so that bit k lands on bit 3k
-__device__ __forceinline__ uint64_t spread3(uint32_t v)
+__host__ __device__ __forceinline__ uint64_t spread3(uint32_t v)
 {
     uint64_t x = v & 0x1fffffu;
     x = (x | (x << 32)) & 0x1f00000000ffffull;
@@ -119,6 +177,43 @@ __device__ __forceinline__ uint64_t spread3(uint32_t v)
     x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
     x = (x | (x << 2)) & 0x1249249249249249ull;
     return x;
+}
+
+// Hilbert index of a cell (16 bits per axis), by Skilling's transform
+// ("Programming the Hilbert curve", AIP Conf. Proc. 707, 2004): the axes are
+// turned into the transposed index by undoing the curve's inversions and
+// exchanges level by level, Gray-decoded, then interleaved x-major.  Every
+// 3k-bit prefix of the key is one octree cell of level k, as with a Morton
+// key, so the radix tree over sorted keys is built the same way; consecutive
+// keys are always face-adjacent cells, so 32 consecutive particles are more
+// compact than in Morton order.
+__host__ __device__ __forceinline__ uint64_t hilbert_key48(uint32_t x, uint32_t y, uint32_t z)
+{
+    uint32_t X[3] = {x, y, z};
+#pragma unroll
+    for (uint32_t Q = 1u << 15; Q > 1; Q >>= 1) {
+        const uint32_t P = Q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & Q) {
+                X[0] ^= P;  // invert
+            } else {        // exchange the low bits of X[0] and X[i]
+                const uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    uint32_t t = 0;
+#pragma unroll
+    for (uint32_t Q = 1u << 15; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    return (spread3(X[0]) << 2) | (spread3(X[1]) << 1) | spread3(X[2]);
 }
 
 // ---- warp helpers -------------------------------------------------------------

@@ -5,10 +5,14 @@
 // clumping_tree_main.cpp:578-600) and the write_mesh_separate normalisation
 // (coarse_mesh.cpp:158-171).
 //
-// Per particle and per cell the weight is bit-identical to the reference:
-// cell range [left, right) per axis from the reference's float expression
-// ((x -+ h)/boxsize)*nc, k = ker_integ(s1, s1 + ds) with s1 = (i*dx - x)*hinv,
-// ker3 = (k0*k1)*k2.
+// Per particle and per cell: the cell range [left, right) per axis is the
+// reference's float expression ((x -+ h)/boxsize)*nc, and ker3 = (k0*k1)*k2 as
+// in the reference; each 1-D weight k is the tent's integral over the cell,
+// evaluated more accurately than the reference's ker_integ(s1, s1 + ds): the
+// cell edges' offsets are fma(i, dx, -x)*hinv and the integral uses
+// cancellation-free forms (tent_integral_rn).  The reference's float weights
+// err by up to 1.1e-5 relative in a mesh cell against FP64 on the 256^3 cube
+// (a halo particle's sliver weight in a thin cell); these stay near 1e-6.
 //
 // Sort by target tile, then gather; deterministic, no atomics on the mesh.
 //  (1) k_dep_prep: one record per particle with x, hinv and the normalised
@@ -426,7 +430,6 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                     const float lo[3] = {B.x, B.y, B.z};
                     const float hi[3] = {Cc.x, Cc.y, Cc.z};
                     const float hinv = A.w;
-                    const float ds = __fmul_rn(J.dx, hinv);  // coarse_mesh.cpp:80
                     float* wl = S.w[lane];
                     uint32_t r = 0;
 #pragma unroll
@@ -436,12 +439,18 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                         const int sh = k * nc + g.O[a];
                         const int r0 = max(ar.left - sh, 0), r1 = min(ar.right - sh, g.E[a]);
                         r |= (uint32_t)((r0 & 15) | ((max(r1, r0) & 15) << 4)) << (8 * a);
-                        // (float) of the unwrapped cell index t + sh, stepped by exact float
-                        // additions (|index| < 2^24) instead of one conversion per cell
+                        // cell t covers [fi*dx, (fi+1)*dx] for the unwrapped cell index
+                        // fi = t + sh (exact float steps, |index| < 2^24); each edge's
+                        // offset from the particle in units of h is fma(fi, dx, -x) * hinv
+                        // (one rounding before the scaling; the reference's s1 and
+                        // s1 + ds, coarse_mesh.cpp:80-90, round i*dx first)
                         float fi = (float)(r0 + sh);
-                        for (int t = r0; t < r1; ++t, fi = __fadd_rn(fi, 1.0f)) {
-                            const float s1 = __fmul_rn(__fsub_rn(__fmul_rn(fi, J.dx), xs[a]), hinv);
-                            wl[a * TS + t] = ker_integ_rn(s1, __fadd_rn(s1, ds));
+                        float e0 = __fmul_rn(__fmaf_rn(fi, J.dx, -xs[a]), hinv);
+                        for (int t = r0; t < r1; ++t) {
+                            fi = __fadd_rn(fi, 1.0f);
+                            const float e1 = __fmul_rn(__fmaf_rn(fi, J.dx, -xs[a]), hinv);
+                            wl[a * TS + t] = tent_integral_rn(e0, e1);
+                            e0 = e1;
                         }
                     }
                     rect = r | ((uint32_t)(__float_as_int(D.z) & FLAG_HALO) << 24);

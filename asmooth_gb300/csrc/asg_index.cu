@@ -1,19 +1,23 @@
 // asg_index.cu -- the spatial index that replaces KDTreeSimple
-// (kdtree_balanced.cpp:212-296): particles are put in 48-bit Morton order by a
-// stable LSD radix sort (each 8-bit digit pass is a counting sort: per-tile
+// (kdtree_balanced.cpp:212-296): particles are put in 48-bit Hilbert order
+// (16 bits per axis; Morton order with ASG_SPACE_CURVE=morton) by a stable LSD
+// radix sort (each 8-bit digit pass is a counting sort: per-tile
 // digit histograms built with warp-aggregated shared-memory atomics, one
 // exclusive scan, a stable scatter), then a radix tree (Karras 2012) is built
 // over the sorted keys with AABBs computed bottom-up.
 //
 // Determinism: the sort is stable and starts from input order, so equal keys
 // stay in input-index order; the tree is a pure function of the sorted keys.
+#include <cstdlib>
+#include <cstring>
+
 #include "asg_common.cuh"
 #include "asg_internal.h"
 
 namespace asg {
 
 // ---------------------------------------------------------------------------
-// unpack + Morton keys
+// unpack + space-filling-curve keys
 // ---------------------------------------------------------------------------
 struct ParticleRec {  // struct Particle (basic_types.h:10-15), 36 bytes
     float x[3], v[3];
@@ -148,11 +152,12 @@ __global__ void k_bounds(const float4* __restrict__ pos, int n, int* lohi)
     }
 }
 
-// Morton key of each particle: 16 bits per axis over [left, right), with the
-// bounds either given (lohi == nullptr) or read from k_bounds' output
-__global__ void k_morton(const float4* __restrict__ pos, int n, float left, float right,
-                         const int* __restrict__ lohi, uint64_t prefix,
-                         uint64_t* __restrict__ keys, int* __restrict__ vals)
+// space-filling-curve key of each particle: 16 bits per axis over [left,
+// right), with the bounds either given (lohi == nullptr) or read from
+// k_bounds' output; Hilbert order, or Morton order with hilbert == 0
+__global__ void k_space_keys(const float4* __restrict__ pos, int n, float left, float right,
+                             const int* __restrict__ lohi, uint64_t prefix, int hilbert,
+                             uint64_t* __restrict__ keys, int* __restrict__ vals)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -168,13 +173,25 @@ __global__ void k_morton(const float4* __restrict__ pos, int n, float left, floa
         t = fminf(fmaxf(t, 0.0f), 65535.0f);
         return (uint32_t)t;
     };
-    keys[i] = (prefix << 48) | spread3(cell(p.x)) | (spread3(cell(p.y)) << 1) |
-              (spread3(cell(p.z)) << 2);
+    const uint32_t cx = cell(p.x), cy = cell(p.y), cz = cell(p.z);
+    const uint64_t k = hilbert ? hilbert_key48(cx, cy, cz)
+                               : spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2);
+    keys[i] = (prefix << 48) | k;
     vals[i] = i;
 }
 
-void launch_morton(const float4* pos_in, int n, float left, float right, int* d_lohi,
-                   uint64_t key_prefix, uint64_t* keys, int* vals, cudaStream_t s)
+// ASG_SPACE_CURVE=morton selects Morton order (a tuning and comparison knob)
+static int use_hilbert()
+{
+    static const int h = [] {
+        const char* e = std::getenv("ASG_SPACE_CURVE");
+        return (e && std::strcmp(e, "morton") == 0) ? 0 : 1;
+    }();
+    return h;
+}
+
+void launch_space_keys(const float4* pos_in, int n, float left, float right, int* d_lohi,
+                       uint64_t key_prefix, uint64_t* keys, int* vals, cudaStream_t s)
 {
     if (n <= 0) return;
     if (d_lohi) {
@@ -182,8 +199,8 @@ void launch_morton(const float4* pos_in, int n, float left, float right, int* d_
         k_bounds<<<min((n + 255) / 256, 1216), 256, 0, s>>>(pos_in, n, d_lohi);
         count_launches(2);
     }
-    k_morton<<<(n + 255) / 256, 256, 0, s>>>(pos_in, n, left, right, d_lohi, key_prefix, keys,
-                                              vals);
+    k_space_keys<<<(n + 255) / 256, 256, 0, s>>>(pos_in, n, left, right, d_lohi, key_prefix,
+                                                  use_hilbert(), keys, vals);
     count_launches(1);
 }
 

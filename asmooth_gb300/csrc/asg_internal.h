@@ -2,14 +2,13 @@
 // translation units of libasmooth_gb300.so (not part of the public C ABI).
 //
 // Data layout in HBM (one particle set, N particles):
-//   pos   float4[N]  x, y, z, w = input index (int bits)   -- Morton order
-//   vel   float4[N]  vx, vy, vz, dens                        -- Morton order
-//   igrp  int[N]                                             -- Morton order
-//   rk    float[N], t33 float[N], idx33 int[N]               -- Morton order
-// Radix tree over the N sorted Morton keys (Karras 2012), N-1 internal nodes:
+//   pos   float4[N]  x, y, z, w = input index (int bits)   -- Hilbert order
+//   vel   float4[N]  vx, vy, vz, dens                        -- Hilbert order
+//   igrp  int[N]                                             -- Hilbert order
+//   rk    float[N], t33 float[N], idx33 int[N]               -- Hilbert order
+// Radix tree over the N sorted space-filling-curve keys (Karras 2012), N-1 internal nodes:
 //   meta  int4[N-1]  child0, child1 (>=0 internal, <0 leaf ~i), first, last
 //   blo/bhi float4[N-1]  AABB of the node's particles
-//   elo/ehi float4[N-1]  AABB of the node's [x-h', x+h'] boxes (after kNN)
 #pragma once
 
 #include <cstddef>
@@ -50,11 +49,11 @@ void launch_unpack_soa(const float* x, const float* v, const float* dens, const 
 void launch_unpack_quant(const int* cell, const uint16_t* off, const float* v, int n, int grid,
                          float left, float cs, float4* pos_in, float4* vel_in, int* igrp_in,
                          float* rk_in, int* err, cudaStream_t s);
-// 48-bit Morton keys (16 bits per axis) over [left, right)^3, or over the
-// particles' own bounding cube when d_lohi (2 ints of scratch) is given;
-// key_prefix lands in bits 48+ (batched cubes)
-void launch_morton(const float4* pos_in, int n, float left, float right, int* d_lohi,
-                   uint64_t key_prefix, uint64_t* keys, int* vals, cudaStream_t s);
+// 48-bit Hilbert keys (16 bits per axis; Morton with ASG_SPACE_CURVE=morton)
+// over [left, right)^3, or over the particles' own bounding cube when d_lohi
+// (2 ints of scratch) is given; key_prefix lands in bits 48+ (batched cubes)
+void launch_space_keys(const float4* pos_in, int n, float left, float right, int* d_lohi,
+                       uint64_t key_prefix, uint64_t* keys, int* vals, cudaStream_t s);
 // stable LSD radix sort of (keys, vals) on the low `bits` bits; ping-pong buffers;
 // returns which buffer (0/1) holds the result
 size_t radix_sort_temp_bytes(int n);

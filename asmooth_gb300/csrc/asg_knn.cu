@@ -29,6 +29,10 @@
 
 namespace asg {
 
+#ifndef KNN_FASTBOX
+#define KNN_FASTBOX 1
+#endif
+
 constexpr int KNN_WARPS = 4;
 // k_knn_t33 runs in blocks of 2 warps, 16 per SM at 64 registers: a warp that
 // finishes early frees its slot sooner than in a block of 4 (23.07 against
@@ -123,11 +127,18 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
                                      __float_as_int(r0.z), __float_as_int(r0.w));
             if (m.w - m.z + 1 > t.leaf) {
+#if KNN_FASTBOX
+                const float d0 = rec_fast0(xq, r1, r2);
+                const float d1 = rec_fast1(xq, r2, r3);
+                const float bound = prune_bound(a[K_NN - 1]);
+#else
                 const float d0 = rec_dist0(xq, r1, r2);
                 const float d1 = rec_dist1(xq, r2, r3);
+                const float bound = a[K_NN - 1];
+#endif
                 // a node whose distance equals a[32] can hold a tie: visit it
-                const bool v0 = __any_sync(FULL, d0 <= a[K_NN - 1]);
-                const bool v1 = __any_sync(FULL, d1 <= a[K_NN - 1]);
+                const bool v0 = __any_sync(FULL, d0 <= bound);
+                const bool v1 = __any_sync(FULL, d1 <= bound);
                 const bool c0_near = __popc(__ballot_sync(FULL, d0 <= d1)) >= 16;
                 const int nn = c0_near ? m.x : m.y, ff = c0_near ? m.y : m.x;
                 const bool vn = c0_near ? v0 : v1, vf = c0_near ? v1 : v0;
@@ -143,8 +154,13 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             first = m.z;
             last = m.w;
             // thresholds may have shrunk since the push: re-test the bucket
+#if KNN_FASTBOX
+            const float db = rec_fast0(xq, r1, r2);
+            if (!__any_sync(FULL, db <= prune_bound(a[K_NN - 1]))) continue;
+#else
             const float db = rec_dist0(xq, r1, r2);
             if (!__any_sync(FULL, db <= a[K_NN - 1])) continue;
+#endif
         }
         if (blist && lane == 0) {
             const int k = nlist[warp];
@@ -190,6 +206,14 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
     }
 }
 
+// The 33rd key of flagged queries: with the exact radius T = t33 each lane
+// counts L = #(d2 < T) and collects the tied indices (d2 == T); the 33rd key is
+// the (33 - L)-th smallest tied index.  A pass keeps the TIE_MAX smallest tied
+// indices above a floor (registers, an insertion network); a lane that needs a
+// deeper one runs another pass with the floor at its last kept index, so any
+// number of ties resolves in at most TIE_PASSES = ceil(33 / TIE_MAX) passes.
+constexpr int TIE_PASSES = (K_NN + TIE_MAX - 1) / TIE_MAX;
+
 __global__ void __launch_bounds__(KNN_WARPS * 32)
 k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
            int* __restrict__ idx33, int all, int* err)
@@ -207,78 +231,95 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
     const float4 xq = pos[q];
     const float T = t33[q];
     int nless = 0, neq = 0;
+    int need = 0;          // rank of the wanted index among the ties above floor
+    int floor_idx = -1;    // this pass keeps tied indices > floor_idx
+    bool open = want;      // this lane still looks for its index
+    int result = -1;
     int tie[TIE_MAX];
-#pragma unroll
-    for (int k = 0; k < TIE_MAX; ++k) tie[k] = INT_MAX;
-
     int* st = stk[warp];
-    if (lane == 0) st[0] = tree_root(n);
-    int sp = 1;
-    bool overflow = false;
-    __syncwarp();
-    while (sp > 0) {
-        const int node = st[--sp];
-        __syncwarp();
-        int first, last;
-        if (node < 0) {
-            first = last = ~node;
-        } else {
-            const float4* rp = t.rec + 4 * (size_t)node;
-            const float4 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3];
-            const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
-                                     __float_as_int(r0.z), __float_as_int(r0.w));
-            if (m.w - m.z + 1 > t.leaf) {
-                const bool v0 = __any_sync(FULL, rec_dist0(xq, r1, r2) <= T);
-                const bool v1 = __any_sync(FULL, rec_dist1(xq, r2, r3) <= T);
-                if (sp + 2 > STACK_MAX) { overflow = true; break; }
-                if (lane == 0) {
-                    if (v1) st[sp] = m.y;
-                    if (v0) st[sp + (v1 ? 1 : 0)] = m.x;
-                }
-                sp += (v0 ? 1 : 0) + (v1 ? 1 : 0);
-                __syncwarp();
-                continue;
-            }
-            first = m.z;
-            last = m.w;
-        }
-        const int cnt = last - first + 1;
-        if (lane < cnt) cand[warp][lane] = pos[first + lane];
-        __syncwarp();
-        for (int j = 0; j < cnt; ++j) {
-            const float4 c = cand[warp][j];
-            const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
-            nless += d2 < T ? 1 : 0;
-            const bool eq = d2 == T;
-            if (__any_sync(FULL, eq)) {
-                neq += eq ? 1 : 0;
-                int v = eq ? __float_as_int(c.w) : INT_MAX;
+
+    for (int pass = 0; pass < TIE_PASSES; ++pass) {
+        if (!__any_sync(FULL, open)) break;
 #pragma unroll
-                for (int k = 0; k < TIE_MAX; ++k) {
-                    const int lo = min(tie[k], v);
-                    v = max(tie[k], v);
-                    tie[k] = lo;
+        for (int k = 0; k < TIE_MAX; ++k) tie[k] = INT_MAX;
+        if (lane == 0) st[0] = tree_root(n);
+        int sp = 1;
+        bool overflow = false;
+        __syncwarp();
+        while (sp > 0) {
+            const int node = st[--sp];
+            __syncwarp();
+            int first, last;
+            if (node < 0) {
+                first = last = ~node;
+            } else {
+                const float4* rp = t.rec + 4 * (size_t)node;
+                const float4 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3];
+                const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
+                                         __float_as_int(r0.z), __float_as_int(r0.w));
+                if (m.w - m.z + 1 > t.leaf) {
+                    const bool v0 = __any_sync(FULL, open && rec_dist0(xq, r1, r2) <= T);
+                    const bool v1 = __any_sync(FULL, open && rec_dist1(xq, r2, r3) <= T);
+                    if (sp + 2 > STACK_MAX) { overflow = true; break; }
+                    if (lane == 0) {
+                        if (v1) st[sp] = m.y;
+                        if (v0) st[sp + (v1 ? 1 : 0)] = m.x;
+                    }
+                    sp += (v0 ? 1 : 0) + (v1 ? 1 : 0);
+                    __syncwarp();
+                    continue;
+                }
+                first = m.z;
+                last = m.w;
+            }
+            const int cnt = last - first + 1;
+            if (lane < cnt) cand[warp][lane] = pos[first + lane];
+            __syncwarp();
+            for (int j = 0; j < cnt; ++j) {
+                const float4 c = cand[warp][j];
+                const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
+                if (pass == 0) nless += d2 < T ? 1 : 0;
+                const int ci = __float_as_int(c.w);
+                const bool eq = open && d2 == T && ci > floor_idx;
+                if (__any_sync(FULL, eq)) {
+                    if (pass == 0) neq += eq ? 1 : 0;
+                    int v = eq ? ci : INT_MAX;
+#pragma unroll
+                    for (int k = 0; k < TIE_MAX; ++k) {
+                        const int lo = min(tie[k], v);
+                        v = max(tie[k], v);
+                        tie[k] = lo;
+                    }
                 }
             }
+            __syncwarp();
         }
-        __syncwarp();
-    }
-    if (overflow) {
-        if (lane == 0) atomicOr(err, ERR_STACK);
-        return;
-    }
-    if (want) {
-        const int need = K_NN - nless;  // position of the 33rd key among the ties
-        int r = -1;
-        if (need < 1 || need > neq) atomicOr(err, ERR_FEW);
-        else if (need > TIE_MAX) atomicOr(err, ERR_TIES);
-        else {
+        if (overflow) {
+            if (lane == 0) atomicOr(err, ERR_STACK);
+            return;
+        }
+        if (open) {
+            if (pass == 0) {
+                need = K_NN - nless;  // position of the 33rd key among all the ties
+                if (need < 1 || need > neq) {
+                    atomicOr(err, ERR_FEW);
+                    open = false;
+                }
+            }
+            if (open && need <= TIE_MAX) {
 #pragma unroll
-            for (int k = 0; k < TIE_MAX; ++k)
-                if (k == need - 1) r = tie[k];
+                for (int k = 0; k < TIE_MAX; ++k)
+                    if (k == need - 1) result = tie[k];
+                open = false;
+            } else if (open) {
+                // the wanted index lies above the TIE_MAX kept ones
+                need -= TIE_MAX;
+                floor_idx = tie[TIE_MAX - 1];
+            }
         }
-        idx33[base + lane] = r;
     }
+    if (open) atomicOr(err, ERR_TIES);  // unreachable: need <= 33 <= TIE_PASSES * TIE_MAX
+    if (want) idx33[base + lane] = result;
 }
 
 // dens is summed exactly, in any order, as 64-bit fixed point per receiver j:

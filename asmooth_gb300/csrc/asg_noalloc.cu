@@ -186,7 +186,7 @@ extern "C" int asg_neighbor_search_noalloc(const float* d_x, int np, float left,
     }
     launch_unpack_soa(d_x, nullptr, d_dens, nullptr, np, F4(L.pos_in), F4(L.vel_in), I(L.igrp_in),
                       F(L.rk_in), err, s);
-    launch_morton(F4(L.pos_in), np, left, right, nullptr, 0,
+    launch_space_keys(F4(L.pos_in), np, left, right, nullptr, 0,
                   reinterpret_cast<uint64_t*>(b + L.keys0), I(L.vals0), s);
     const int cur = radix_sort(reinterpret_cast<uint64_t*>(b + L.keys0), I(L.vals0),
                                reinterpret_cast<uint64_t*>(b + L.keys1), I(L.vals1), np, 48,

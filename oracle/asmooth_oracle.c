@@ -47,6 +47,29 @@ static inline float ker_integ(float x1, float x2)
     const float fac2 = (float)(-1 + 2 * (x2 > 0.0f));
     return fac2 * tent_f(fac2 * x2) - fac1 * tent_f(fac1 * x1);
 }
+/* The library's cell weight (asg_common.cuh tent_integral_rn): the tent's
+ * integral over [a, b] in cancellation-free forms, every operation rounded
+ * as written (-ffp-contract=off), and the cell edge's offset from the particle
+ * in units of h, fma(i, dx, -x) * hinv. */
+static inline float tent_pos(float t) { return t >= 1.0f ? 0.5f : t * (1.0f - 0.5f * t); }
+static inline float tent_integral(float a, float b)
+{
+    if (a >= 1.0f || b <= -1.0f) return 0.0f;
+    if (a >= 0.0f) {
+        if (b >= 1.0f) { const float u = 1.0f - a; return 0.5f * u * u; }
+        return (b - a) * (1.0f - 0.5f * (a + b));
+    }
+    if (b <= 0.0f) {
+        if (a <= -1.0f) { const float u = 1.0f + b; return 0.5f * u * u; }
+        return (b - a) * (1.0f + 0.5f * (a + b));
+    }
+    return tent_pos(b) + tent_pos(-a);
+}
+static inline float edge_off(int i, float dx, float x, float hinv) { return fmaf((float)i, dx, -x) * hinv; }
+static inline float lib_weight(int i, float dx, float x, float hinv)
+{
+    return tent_integral(edge_off(i, dx, x, hinv), edge_off(i + 1, dx, x, hinv));
+}
 static inline double tent_f64(double x) { return x >= 1.0 ? 0.5 : x - 0.5 * x * x; }
 static inline double ker_integ64(double x1, double x2)
 {
@@ -499,9 +522,10 @@ static int dep_range(const float* y, float h, float boxsize, int nc, int periodi
  * its contributions in the serial loop's order and the float mesh is the
  * serial one bit for bit.  The FP64 totals are summed per plane, then over
  * the planes in order.  mesh64 holds the FP64 restatement (weights computed in
- * double), or with fw the FP64 sums of the reference's float weights ker3,
- * ker3*dens and ker3*v (products exact in double).  Returns -4 if some rk is
- * not positive. */
+ * double), or with fw the FP64 sums of the library's float weights
+ * (lib_weight: ker3 = (k0*k1)*k2, ker3*dens and ker3*v, products exact in
+ * double), and the totals are then those weights' FP64 sums.  Returns -4 if
+ * some rk is not positive. */
 static int dep_by_planes(const float* x, const float* v, const float* dens, const float* rk,
                          const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
                          const float off[3], int nthreads, float* mesh, double* mesh64,
@@ -560,11 +584,13 @@ static int dep_by_planes(const float* x, const float* v, const float* dens, cons
             const int to_halo = sign * igrp[j] > 0;
             float s1 = (iz * dx - xp[2]) * hinv;
             const float k2 = ker_integ(s1, s1 + ds);
+            const float l2 = fw ? lib_weight(iz, dx, xp[2], hinv) : 0.0f;
             double t64 = ((double)iz * (double)dx - (double)xp[2]) * hinv64;
             const double k2d = ker_integ64(t64, t64 + ds64);
             for (int iy = lo[1]; iy < hi[1]; ++iy) {
                 s1 = (iy * dx - xp[1]) * hinv;
                 const float k1 = ker_integ(s1, s1 + ds);
+                const float l1 = fw ? lib_weight(iy, dx, xp[1], hinv) : 0.0f;
                 t64 = ((double)iy * (double)dx - (double)xp[1]) * hinv64;
                 const double k1d = ker_integ64(t64, t64 + ds64);
                 for (int ix = lo[0]; ix < hi[0]; ++ix) {
@@ -573,20 +599,21 @@ static int dep_by_planes(const float* x, const float* v, const float* dens, cons
                     const size_t idx = (size_t)p * nc2 + (size_t)((iy % nc + nc) % nc) * nc +
                                        (size_t)((ix % nc + nc) % nc);
                     const float ker3 = k0 * k1 * k2;
+                    const float lw3 = fw ? lib_weight(ix, dx, xp[0], hinv) * l1 * l2 : 0.0f;
                     if (!to_halo) {
                         mn[idx] += ker3;
                         mc[idx] += ker3 * dens[j];
                         mv[3 * idx] += ker3 * v[3 * (size_t)j];
                         mv[3 * idx + 1] += ker3 * v[3 * (size_t)j + 1];
                         mv[3 * idx + 2] += ker3 * v[3 * (size_t)j + 2];
-                        tn += (double)ker3;
+                        tn += fw ? (double)lw3 : (double)ker3;
                     } else {
                         mh[idx] += ker3;
-                        th += (double)ker3;
+                        th += fw ? (double)lw3 : (double)ker3;
                     }
                     if (mesh64) {
                         t64 = ((double)ix * (double)dx - (double)xp[0]) * hinv64;
-                        const double w = fw ? (double)ker3 : ker_integ64(t64, t64 + ds64) * k1d * k2d;
+                        const double w = fw ? (double)lw3 : ker_integ64(t64, t64 + ds64) * k1d * k2d;
                         if (!to_halo) {
                             mesh64[idx] += w;
                             mesh64[2 * nmesh + idx] += w * (double)dens[j];
@@ -756,9 +783,10 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
     return bad ? -4 : 0;
 }
 
-/* As orc_assign_on_mesh (float mesh the same bit for bit), with mesh64 the
- * FP64 sums of the reference's float weights instead of the FP64 restatement:
- * the value a deposit that sums those weights without rounding error gives. */
+/* As orc_assign_on_mesh (float mesh the same bit for bit), with mesh64 and the
+ * totals the FP64 sums of the library's float weights (lib_weight) instead of
+ * the FP64 restatement: what a deposit that sums those weights without
+ * rounding error gives. */
 int orc_assign_on_mesh_fw(const float* x, const float* v, const float* dens, const float* rk,
                           const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
                           const float* offset, int nthreads, float* mesh, double* mesh64,

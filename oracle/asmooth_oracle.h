@@ -66,7 +66,7 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
                        float* mesh, double* mesh64, double* totals);
 
 /* n-channel-only variant (coarse_mesh.cpp:212-269). mesh has nc^3 floats. */
-/* as orc_assign_on_mesh; mesh64 = FP64 sums of the reference's float weights */
+/* as orc_assign_on_mesh; mesh64, totals = FP64 sums of the library's float weights */
 int orc_assign_on_mesh_fw(const float* x, const float* v, const float* dens, const float* rk,
                           const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
                           const float* offset, int nthreads, float* mesh, double* mesh64,

@@ -102,9 +102,10 @@ class Oracle:
     # -- mesh ----------------------------------------------------------------
     def assign_on_mesh(self, x, v, dens, rk, igrp, boxsize, nc, sign=-1, periodic=False,
                        offset=(0.0, 0.0, 0.0), nthreads=1, want64=True, float_weights=False):
-        """(float mesh, FP64 mesh, FP64 totals).  The FP64 mesh is the FP64
-        restatement, or with float_weights the FP64 sums of the reference's
-        float weights (ker3, ker3*dens, ker3*v)."""
+        """(float mesh, FP64 mesh, FP64 totals).  The float mesh is the
+        reference's; the FP64 mesh is the FP64 restatement, or with
+        float_weights the FP64 sums of the library's float weights (its more
+        accurate evaluation of the tent integrals: ker3, ker3*dens, ker3*v)."""
         x = np.ascontiguousarray(x, np.float32)
         n = x.shape[0]
         mesh = np.zeros(6 * nc ** 3, np.float32)

@@ -4,46 +4,39 @@ box faces (clipping), halo and non-halo particles under both signs, in the
 plain (coarse_mesh.cpp:45-127), periodic (global_mesh.cpp:25-123) and
 density-only (coarse_mesh.cpp:212-269) deposits.
 
-Two checks, both through the C ABI:
+The library evaluates each cell's tent integral more accurately than the
+reference's float ker_integ (coarse_mesh.cpp:10-22, 80-90): cell edges as
+fma(i, dx, -x) * hinv and cancellation-free forms of the integral.  The oracle
+restates those float operations in C (lib_weight).  Three checks, all through
+the C ABI:
   * disjoint supports: the particles are split into batches whose cell boxes
-    do not overlap, so every cell receives at most one weight; then every
-    channel equals the reference's float mesh (the oracle restatement, pinned
-    bit for bit to the reference on these inputs on the CPU) bit for bit: each
-    per-cell weight ker3 = (k0*k1)*k2 and each product with dens and v is the
-    reference's float value;
+    do not overlap, so every cell receives at most one weight; every channel
+    then equals the oracle's restatement bit for bit (ker3, ker3*dens, ker3*v
+    each correctly rounded);
   * the whole set at once: n, c and halo are the correctly rounded FP64 sums of
-    the reference's float weights (error at most 2^-24 relative plus the
-    double-float accumulation's 2^-38), v within 1e-5 of |v| + n, and the FP64
-    mass totals within 1e-12 of the FP64 sums of the float weights."""
+    those float weights (error at most 2^-24 relative plus the double-float
+    accumulation's 2^-38), v within 1e-5 of |v| + n, and the FP64 mass totals
+    within 1e-12 of the FP64 sums of the float weights;
+  * accuracy: every channel within 1e-5 of the FP64 restatement (cells above
+    1e-3 of the mean density), the bar the reference's own float weights miss
+    on these inputs."""
 import numpy as np
 import pytest
+
+from helpers import EDGE_L as L, EDGE_NCS as NCS, edge_inputs, field_errors
 
 from asmooth_gb300 import api
 
 pytestmark = pytest.mark.gpu
 
-L = 64.0
-NCS = (16, 32)  # cells of 4 and 2 units; 8-cell tiles of 32 and 16 units
 ROUND_TOL = 2.0 ** -24 + 2.0 ** -38
 V_TOL = 1e-5
 TOTAL_TOL = 1e-12
+FIELD_TOL = 1e-5
 
 
 def bits(a):
     return np.asarray(a, np.float32).view(np.int32)
-
-
-def edge_inputs(seed=11, n=400):
-    rng = np.random.default_rng(seed)
-    edges = np.arange(0, 33, dtype=np.float32) * np.float32(2.0)  # every cell edge of nc = 32
-    x = rng.choice(edges, (n, 3)).astype(np.float32)
-    x[:100] += rng.choice([-1e-3, 0.0, 1e-3], (100, 3)).astype(np.float32)  # next to edges
-    x[100:120] = rng.uniform(-3, L + 3, (20, 3)).astype(np.float32)  # past the faces
-    rk = rng.choice(np.float32([2.0, 4.0, 6.0, 8.0, 3.999, 0.5, 1.0]), n).astype(np.float32)
-    v = rng.normal(size=(n, 3)).astype(np.float32)
-    dens = rng.uniform(0.5, 2.0, n).astype(np.float32)
-    igrp = rng.choice([-1, 0, 2], n).astype(np.int32)
-    return x, v, dens, rk, igrp
 
 
 def axis_cells(x, h, nc, periodic):
@@ -88,17 +81,16 @@ def gpu_mesh(ctx, mode, x, v, dens, rk, igrp, nc, sign):
     return ctx.assign_on_density_mesh(p, L, nc, sign), None
 
 
-def oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign):
-    """(float mesh, FP64 sums of the float weights, FP64 totals) in the GPU
-    call's layout (density-only: the n channel)."""
+def oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign, float_weights=True):
+    """(FP64 sums of the library's float weights, or the FP64 restatement with
+    float_weights=False; FP64 totals) in the GPU call's layout (density-only:
+    the n channel)."""
     per = mode == "periodic"
-    m, m64, t64 = oracle.assign_on_mesh(x, v, dens, rk, igrp, L, nc, sign, periodic=per,
-                                        offset=(L, 0.0, 2 * L), float_weights=True)
+    _, m64, t64 = oracle.assign_on_mesh(x, v, dens, rk, igrp, L, nc, sign, periodic=per,
+                                        offset=(L, 0.0, 2 * L), float_weights=float_weights)
     if mode == "density":
-        d = oracle.assign_on_density_mesh(x, rk, igrp, L, nc, sign)
-        assert np.array_equal(bits(d), bits(m[: nc ** 3]))  # the n channel of the plain deposit
-        return d, m64[: nc ** 3], t64
-    return m, m64, t64
+        return m64[: nc ** 3], t64
+    return m64, t64
 
 
 @pytest.mark.parametrize("mode", ["plain", "periodic", "density"])
@@ -111,18 +103,18 @@ def test_deposit_edges(gpu_ctx, oracle, mode, sign, nc):
         x, v, dens, rk, igrp = x[inside], v[inside], dens[inside], rk[inside], igrp[inside]
     nm = nc ** 3
 
-    # one weight per cell: bit for bit the reference's float mesh
+    # one weight per cell: bit for bit the oracle's restatement of the float weights
     batches = disjoint_batches(x, rk, nc, mode == "periodic")
     assert len(batches) < len(x)  # the batches do combine particles
     for b in batches:
         b = np.asarray(b)
         got, _ = gpu_mesh(gpu_ctx, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
-        ref, _, _ = oracle_mesh(oracle, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
-        assert np.array_equal(bits(got), bits(ref)), (mode, sign, nc, b[:4])
+        s64, _ = oracle_mesh(oracle, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
+        assert np.array_equal(bits(got), bits(s64.astype(np.float32))), (mode, sign, nc, b[:4])
 
     # the whole set: correctly rounded FP64 sums of the float weights
     got, tot = gpu_mesh(gpu_ctx, mode, x, v, dens, rk, igrp, nc, sign)
-    _, s64, t64 = oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign)
+    s64, t64 = oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign)
     chans = [(0, nm)] if mode == "density" else [(0, nm), (nm, 2 * nm), (2 * nm, 3 * nm)]
     for a, e in chans:
         g, s = got[a:e].astype(np.float64), s64[a:e]
@@ -133,3 +125,8 @@ def test_deposit_edges(gpu_ctx, oracle, mode, sign, nc):
         assert np.all(np.abs(got[3 * nm:].astype(np.float64) - vs) <= V_TOL * scale + 1e-30)
         for k in range(2):
             assert abs(tot[k] - t64[k]) <= TOTAL_TOL * max(abs(t64[k]), 1e-300), (k, tot, t64)
+
+    # accuracy against the FP64 restatement of the weights
+    e64, _ = oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign, float_weights=False)
+    errs = field_errors(got, e64, nc, mode == "density")
+    assert max(errs.values()) <= FIELD_TOL, errs

@@ -63,8 +63,9 @@ def mesh_errors(mesh, m64, nc):
         sel = dens > cut
         out[name] = float(np.max(np.abs(got[sel].astype(np.float64) - ref[sel]) / np.abs(ref[sel]))
                           ) if sel.any() else 0.0
-    scale = np.abs(v64) + np.repeat(n64, 3)
-    out["v"] = float(np.max(np.abs(v.astype(np.float64) - v64) / (scale + 1e-300)))
+    sel = np.repeat(n64 > cut, 3)  # v against |v| + n on the same cells
+    scale = (np.abs(v64) + np.repeat(n64, 3))[sel]
+    out["v"] = float(np.max(np.abs(v.astype(np.float64)[sel] - v64[sel]) / scale))
     return out
 
 

@@ -215,3 +215,29 @@ def test_oracle_matches_reference_on_cell_edges(oracle):
         g_r = R.assign_on_global_mesh(x[inside], v[inside], dens[inside], rk[inside],
                                       igrp[inside], L, nc, sign, coords=(1, 0, 2))
         assert np.array_equal(bits(g_o), bits(g_r))
+
+
+def test_library_weights_within_bar_on_cell_edges(oracle):
+    """The library's cell weights (fma cell edges, cancellation-free tent
+    integrals; the oracle's lib_weight restatement) against the FP64
+    restatement on the adversarial cell-edge inputs: within 1e-5 per cell in
+    every deposit form, where the reference's float weights are not."""
+    from helpers import EDGE_L, EDGE_NCS, edge_inputs, field_errors
+
+    x, v, dens, rk, igrp = edge_inputs()
+    worst_ref = 0.0
+    for periodic in (False, True):
+        xs, vs, ds, rs, gs = x, v, dens, rk, igrp
+        if periodic:
+            m = np.all((x >= 0) & (x < EDGE_L), axis=1)
+            xs, vs, ds, rs, gs = x[m], v[m], dens[m], rk[m], igrp[m]
+        for sign in (-1, 1):
+            for nc in EDGE_NCS:
+                kw = dict(periodic=periodic, offset=(EDGE_L, 0.0, 2 * EDGE_L))
+                ref, e64, _ = oracle.assign_on_mesh(xs, vs, ds, rs, gs, EDGE_L, nc, sign, **kw)
+                _, l64, _ = oracle.assign_on_mesh(xs, vs, ds, rs, gs, EDGE_L, nc, sign,
+                                                  float_weights=True, **kw)
+                lib = field_errors(l64.astype(np.float32), e64, nc, False)
+                assert max(lib.values()) <= 1e-5, lib
+                worst_ref = max(worst_ref, max(field_errors(ref, e64, nc, False).values()))
+    assert worst_ref > 1e-5  # the reference's float weights miss the bar on these inputs
