@@ -16,11 +16,12 @@
 //               -> t33 = 33rd smallest d2 (exact, with multiplicity)
 //   k_knn_ties  exact-radius recount: L = #(d2 < t33), the tied indices
 //               -> idx33 = input index of the 33rd key, rk = sqrtf(t33)
-//   k_dens_scatter each lane is a SOURCE q with its exact radius and adds
-//               ker(q, j) to every j of its 32-set as 64-bit fixed point
-//               (per-receiver power-of-two scale, warp-aggregated integer
-//               atomics): exact integer sums, so deterministic in any order.
-//               It visits the buckets k_knn_t33 recorded for the bundle.
+//   k_dens_scatter the bundle's queries are SOURCES q with their exact radii;
+//               in each bucket a lane holds a receiver j and adds ker(q, j)
+//               for the queries q whose 32-set holds j, as 64-bit fixed point
+//               (per-receiver power-of-two scale, one integer atomic per
+//               receiver and bucket): exact integer sums, so deterministic in
+//               any order.  It visits the buckets k_knn_t33 recorded.
 #include <climits>
 
 #include "asg_common.cuh"
@@ -28,10 +29,6 @@
 #include "asg_knn_net.cuh"
 
 namespace asg {
-
-#ifndef KNN_FASTBOX
-#define KNN_FASTBOX 1
-#endif
 
 constexpr int KNN_WARPS = 4;
 // k_knn_t33 runs in blocks of 2 warps, 16 per SM at 64 registers: a warp that
@@ -127,15 +124,9 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
                                      __float_as_int(r0.z), __float_as_int(r0.w));
             if (m.w - m.z + 1 > t.leaf) {
-#if KNN_FASTBOX
                 const float d0 = rec_fast0(xq, r1, r2);
                 const float d1 = rec_fast1(xq, r2, r3);
                 const float bound = prune_bound(a[K_NN - 1]);
-#else
-                const float d0 = rec_dist0(xq, r1, r2);
-                const float d1 = rec_dist1(xq, r2, r3);
-                const float bound = a[K_NN - 1];
-#endif
                 // a node whose distance equals a[32] can hold a tie: visit it
                 const bool v0 = __any_sync(FULL, d0 <= bound);
                 const bool v1 = __any_sync(FULL, d1 <= bound);
@@ -154,13 +145,8 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             first = m.z;
             last = m.w;
             // thresholds may have shrunk since the push: re-test the bucket
-#if KNN_FASTBOX
             const float db = rec_fast0(xq, r1, r2);
             if (!__any_sync(FULL, db <= prune_bound(a[K_NN - 1]))) continue;
-#else
-            const float db = rec_dist0(xq, r1, r2);
-            if (!__any_sync(FULL, db <= a[K_NN - 1])) continue;
-#endif
         }
         if (blist && lane == 0) {
             const int k = nlist[warp];
@@ -343,12 +329,16 @@ __global__ void k_dens_prep(const float* __restrict__ rk, int n, int* __restrict
     acc[j] = 0ull;
 }
 
-// Each lane is a query q with its exact radius: it visits the candidates j
-// with d2 <= t33_q, and for every j of its 32-set (d2 < t33, or d2 == t33 with
-// index below idx33) the warp adds the members' fixed-point weights and one
-// lane adds the sum to acc[j].  The buckets come from the bundle's list of
-// buckets k_knn_t33 scanned (each re-tested against the exact radii), or from
-// a walk of the tree when the list overflowed or is absent.
+// The warp serves the 32 queries (sources) q of a bundle with their exact radii
+// and visits the buckets k_knn_t33 recorded for the bundle (each re-tested), or
+// walks the tree when the list overflowed or is absent.  In a bucket each lane
+// holds one candidate receiver j, and the warp loops over only the queries
+// whose radius reaches the bucket's box (a ballot; about 9 of 32 on the 256^3
+// cube): for each such q every lane tests whether its j is in q's 32-set
+// ((d2, index) below q's 33rd key) and adds ker(q, j) as 64-bit fixed point to
+// a register; one integer atomic per receiver and bucket adds the sum to
+// acc[j].  The sums are exact integers, so the order of the additions and
+// atomics does not matter.
 __global__ void __launch_bounds__(KNN_WARPS * 32)
 k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
                const int* __restrict__ idx33, const int* __restrict__ blist,
@@ -356,8 +346,8 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
                unsigned long long* __restrict__ acc)
 {
     __shared__ int stk[KNN_WARPS][STACK_MAX];
-    __shared__ float4 cand[KNN_WARPS][32];
-    __shared__ float cscale[KNN_WARPS][32];  // 2^(FIX_BITS - e_j)
+    __shared__ float4 qpos[KNN_WARPS][32];  // x, y, z, t33 of the bundle's queries
+    __shared__ float4 qaux[KNN_WARPS][32];  // hinv, hinv^3, idx33 (int bits)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = t.n;
     const int base = (blockIdx.x * KNN_WARPS + warp) * 32;
@@ -366,33 +356,54 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
     const int q = min(base + lane, n - 1);
     const float4 xq = pos[q];
     const float T = valid ? t33[q] : -1.0f;  // a padding lane takes nothing
-    const int i33 = idx33[q];
     const float hinv = __fdiv_rn(1.0f, rk[q]);
-    const bool any_tie = __any_sync(FULL, valid && i33 >= 0);  // warp-uniform
+    const float bound = prune_bound(T);
+    qpos[warp][lane] = make_float4(xq.x, xq.y, xq.z, T);
+    qaux[warp][lane] = make_float4(hinv, __fmul_rn(__fmul_rn(hinv, hinv), hinv),
+                                   __int_as_float(idx33[q]), 0.0f);
+    __syncwarp();
 
-    // scans bucket [first, last] against every lane's 32-set
-    auto scan = [&](int first, int last) {
+    // the bucket [first, last] (box from its node record, or a single particle)
+    // against the queries of mask M
+    auto scan = [&](int first, int last, unsigned M) {
         const int cnt = last - first + 1;
-        if (lane < cnt) {
-            cand[warp][lane] = pos[first + lane];
-            cscale[warp][lane] = __int_as_float((127 + FIX_BITS - dexp[first + lane]) << 23);
+        const bool have = lane < cnt;
+        const int j = first + (have ? lane : 0);
+        const float4 c = pos[j];
+        const float sc = __int_as_float((127 + FIX_BITS - dexp[j]) << 23);  // 2^(FIX_BITS - e_j)
+        const int cj = __float_as_int(c.w);
+        unsigned long long sum = 0ull;
+        while (M) {
+            const int k = __ffs(M) - 1;
+            M &= M - 1;
+            const float4 Q = qpos[warp][k];
+            const float4 A = qaux[warp][k];
+            // norm2 (nbr_search.cpp:20-25) and ker (:27-37) of (q, j), query first
+            const float dx = __fsub_rn(Q.x, c.x), dy = __fsub_rn(Q.y, c.y), dz = __fsub_rn(Q.z, c.z);
+            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            const bool member = d2 < Q.w || (d2 == Q.w && cj < __float_as_int(A.z));
+            float w = A.y;
+            w = __fmul_rn(w, __fsub_rn(1.0f, __fmul_rn(fabsf(dx), A.x)));
+            w = __fmul_rn(w, __fsub_rn(1.0f, __fmul_rn(fabsf(dy), A.x)));
+            w = __fmul_rn(w, __fsub_rn(1.0f, __fmul_rn(fabsf(dz), A.x)));
+            if (member) sum += __float2ull_rn(__fmul_rn(w, sc));
         }
-        __syncwarp();
-        for (int k = 0; k < cnt; ++k) {
-            const float4 c = cand[warp][k];
-            const float d2 = norm2_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z);
-            // the index rule matters only where the 33rd distance is tied
-            const bool member = d2 < T || (any_tie && d2 == T && __float_as_int(c.w) < i33);
-            if (__any_sync(FULL, member)) {
-                const float w = member ? ker_rn(xq.x, xq.y, xq.z, c.x, c.y, c.z, hinv) : 0.0f;
-                const unsigned long long f = __float2ull_rn(__fmul_rn(w, cscale[warp][k]));
-                const unsigned s0 = __reduce_add_sync(FULL, (unsigned)(f & 0x3fffffull));
-                const unsigned s1 = __reduce_add_sync(FULL, (unsigned)(f >> 22));
-                if (lane == 0)
-                    atomicAdd(&acc[first + k], (unsigned long long)s0 + ((unsigned long long)s1 << 22));
-            }
+        if (have && sum) atomicAdd(&acc[j], sum);
+    };
+    // the queries whose radius reaches a bucket node's box
+    auto reach = [&](int node) -> unsigned {
+        if (node < 0) return __ballot_sync(FULL, valid);
+        const float4* rp = t.rec + 4 * (size_t)node;
+        return __ballot_sync(FULL, rec_fast0(xq, rp[1], rp[2]) <= bound);
+    };
+    auto bucket_range = [&](int node, int& first, int& last) {
+        if (node < 0) {
+            first = last = ~node;
+        } else {
+            const float4 r0 = t.rec[4 * (size_t)node];
+            first = __float_as_int(r0.z);
+            last = __float_as_int(r0.w);
         }
-        __syncwarp();
     };
 
     const int* bl = blist ? blist + (size_t)(base >> 5) * (KNN_LIST + 1) : nullptr;
@@ -409,14 +420,11 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
             for (int w = 1; w < (KNN_LIST + 31) / 32; ++w)
                 if ((i >> 5) == w) v = e[w];
             const int node = __shfl_sync(FULL, v, i & 31);
-            if (node < 0) {
-                scan(~node, ~node);
-                continue;
-            }
-            const float4* rp = t.rec + 4 * (size_t)node;
-            const float4 r0 = rp[0], r1 = rp[1], r2 = rp[2];
-            if (!__any_sync(FULL, rec_dist0(xq, r1, r2) <= T)) continue;
-            scan(__float_as_int(r0.z), __float_as_int(r0.w));
+            const unsigned M = reach(node);
+            if (!M) continue;
+            int first, last;
+            bucket_range(node, first, last);
+            scan(first, last, M);
         }
         return;
     }
@@ -428,10 +436,7 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
     while (sp > 0) {
         const int node = st[--sp];
         __syncwarp();
-        int first, last;
-        if (node < 0) {
-            first = last = ~node;
-        } else {
+        if (node >= 0) {
             const int4 m = t.meta[node];
             if (m.w - m.z + 1 > t.leaf) {
                 const bool v0 = __any_sync(FULL, child_dist2(pos, t, m.x, xq) <= T);
@@ -445,10 +450,12 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
                 __syncwarp();
                 continue;
             }
-            first = m.z;
-            last = m.w;
         }
-        scan(first, last);
+        const unsigned M = reach(node);
+        if (!M) continue;
+        int first, last;
+        bucket_range(node, first, last);
+        scan(first, last, M);
     }
 }
 

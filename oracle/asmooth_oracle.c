@@ -524,8 +524,9 @@ static int dep_range(const float* y, float h, float boxsize, int nc, int periodi
  * the planes in order.  mesh64 holds the FP64 restatement (weights computed in
  * double), or with fw the FP64 sums of the library's float weights
  * (lib_weight: ker3 = (k0*k1)*k2, ker3*dens and ker3*v, products exact in
- * double), and the totals are then those weights' FP64 sums.  Returns -4 if
- * some rk is not positive. */
+ * double).  The totals are always the FP64 sums of the library's float
+ * weights (n and halo), the quantity the library's FP64 totals reproduce.
+ * Returns -4 if some rk is not positive. */
 static int dep_by_planes(const float* x, const float* v, const float* dens, const float* rk,
                          const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
                          const float off[3], int nthreads, float* mesh, double* mesh64,
@@ -534,6 +535,7 @@ static int dep_by_planes(const float* x, const float* v, const float* dens, cons
     const size_t nmesh = (size_t)nc * nc * nc;
     const float dx = boxsize / nc;
     const int nc2 = nc * nc;
+    const int lw = fw || totals;  /* the library's float weights are needed */
     size_t* start = (size_t*)calloc((size_t)nc + 1, sizeof(size_t));
     double* pt = (double*)calloc(2 * (size_t)nc, sizeof(double));
     if (!start || !pt) { free(start); free(pt); return -2; }
@@ -584,13 +586,13 @@ static int dep_by_planes(const float* x, const float* v, const float* dens, cons
             const int to_halo = sign * igrp[j] > 0;
             float s1 = (iz * dx - xp[2]) * hinv;
             const float k2 = ker_integ(s1, s1 + ds);
-            const float l2 = fw ? lib_weight(iz, dx, xp[2], hinv) : 0.0f;
+            const float l2 = lw ? lib_weight(iz, dx, xp[2], hinv) : 0.0f;
             double t64 = ((double)iz * (double)dx - (double)xp[2]) * hinv64;
             const double k2d = ker_integ64(t64, t64 + ds64);
             for (int iy = lo[1]; iy < hi[1]; ++iy) {
                 s1 = (iy * dx - xp[1]) * hinv;
                 const float k1 = ker_integ(s1, s1 + ds);
-                const float l1 = fw ? lib_weight(iy, dx, xp[1], hinv) : 0.0f;
+                const float l1 = lw ? lib_weight(iy, dx, xp[1], hinv) : 0.0f;
                 t64 = ((double)iy * (double)dx - (double)xp[1]) * hinv64;
                 const double k1d = ker_integ64(t64, t64 + ds64);
                 for (int ix = lo[0]; ix < hi[0]; ++ix) {
@@ -599,17 +601,17 @@ static int dep_by_planes(const float* x, const float* v, const float* dens, cons
                     const size_t idx = (size_t)p * nc2 + (size_t)((iy % nc + nc) % nc) * nc +
                                        (size_t)((ix % nc + nc) % nc);
                     const float ker3 = k0 * k1 * k2;
-                    const float lw3 = fw ? lib_weight(ix, dx, xp[0], hinv) * l1 * l2 : 0.0f;
+                    const float lw3 = lw ? lib_weight(ix, dx, xp[0], hinv) * l1 * l2 : 0.0f;
                     if (!to_halo) {
                         mn[idx] += ker3;
                         mc[idx] += ker3 * dens[j];
                         mv[3 * idx] += ker3 * v[3 * (size_t)j];
                         mv[3 * idx + 1] += ker3 * v[3 * (size_t)j + 1];
                         mv[3 * idx + 2] += ker3 * v[3 * (size_t)j + 2];
-                        tn += fw ? (double)lw3 : (double)ker3;
+                        tn += (double)lw3;
                     } else {
                         mh[idx] += ker3;
-                        th += fw ? (double)lw3 : (double)ker3;
+                        th += (double)lw3;
                     }
                     if (mesh64) {
                         t64 = ((double)ix * (double)dx - (double)xp[0]) * hinv64;
@@ -654,14 +656,13 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
     const float off[3] = {periodic && offset ? offset[0] : 0.0f,
                           periodic && offset ? offset[1] : 0.0f,
                           periodic && offset ? offset[2] : 0.0f};
-    double tot_n = 0.0, tot_h = 0.0;
     int bad = 0;
     if (nthreads < 1) nthreads = 1;
     const int par = nthreads > 1 && !mesh64 && !totals;
-    /* the FP64 sums in parallel, deterministically (the float mesh is the
-     * serial loop's); without them the loop below runs with the atomics of the
-     * reference's OpenMP build */
-    if (nthreads > 1 && (mesh64 || totals))
+    /* the FP64 sums (in parallel, deterministically; the float mesh is the
+     * serial loop's); without them the loop below runs serially or with the
+     * atomics of the reference's OpenMP build */
+    if (mesh64 || totals)
         return dep_by_planes(x, v, dens, rk, igrp, n, boxsize, nc, sign, periodic, off, nthreads,
                              mesh, mesh64, totals, 0);
 
@@ -747,7 +748,6 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
                             mv[3 * idx] += ker3 * v[3 * (size_t)j];
                             mv[3 * idx + 1] += ker3 * v[3 * (size_t)j + 1];
                             mv[3 * idx + 2] += ker3 * v[3 * (size_t)j + 2];
-                            tot_n += (double)ker3;
                         }
                     } else {
                         if (par) {
@@ -757,7 +757,6 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
                             mh[idx] += ker3;
                         } else {
                             mh[idx] += ker3;
-                            tot_h += (double)ker3;
                         }
                     }
                     if (mesh64) {
@@ -779,7 +778,6 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
             }
         }
     }
-    if (totals) { totals[0] = tot_n; totals[1] = tot_h; }
     return bad ? -4 : 0;
 }
 

@@ -20,10 +20,15 @@ def test_deposit_reciprocal_division():
         assert (ts ** 3 - 1) * m < 2 ** 31  # no overflow of the int product
 
 
-def test_dens_fixed_point_chunks():
-    """k_dens_scatter sums 32 lanes' 64-bit terms (below 2^44) as two 32-bit
-    warp reductions of 22-bit chunks: neither chunk sum can overflow."""
+def test_dens_fixed_point_sums():
+    """k_dens_scatter adds 64-bit fixed-point terms w * 2^(FIX_BITS - e_j), each
+    below 2^(FIX_BITS + 4) (w <= 8 hinv_j^3 < 2^(e_j + 3), one rounding), in a
+    lane register over at most the 32 queries of a bundle per bucket, then into
+    acc[j] with one atomic: neither the register nor acc can overflow before a
+    receiver collects 2^(60 - FIX_BITS) terms."""
     src = open(os.path.join(CSRC, "asg_knn.cu")).read()
-    assert "f & 0x3fffffull" in src and "f >> 22" in src
-    lo_max, hi_max = 2 ** 22 - 1, (2 ** 44 - 1) >> 22
-    assert 32 * lo_max < 2 ** 32 and 32 * hi_max < 2 ** 32
+    fix = int(re.search(r"constexpr int FIX_BITS = (\d+);", src).group(1))
+    assert "sum += __float2ull_rn(__fmul_rn(w, sc));" in src
+    term = 2 ** (fix + 4)
+    assert 32 * term < 2 ** 64
+    assert 2 ** (60 - fix) * term <= 2 ** 64 and 2 ** (60 - fix) >= 2 ** 20
