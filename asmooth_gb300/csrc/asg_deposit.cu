@@ -31,6 +31,8 @@
 // n, c and halo are double-float (two-sum) sums, so the per-tile FP64 totals
 // reproduce the FP64 sum of the float weights.
 #include <atomic>
+#include <cstdlib>
+#include <cstring>
 
 #include "asg_common.cuh"
 #include "asg_internal.h"
@@ -527,11 +529,316 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
 }
 
 // ---------------------------------------------------------------------------
+// (4') the same work items on the tensor cores
+// ---------------------------------------------------------------------------
+// A pair's contribution to its tile is separable: weight wx[x] wy[y] wz[z]
+// times the particle's value in each channel (n: 1, halo: 1, c: dens, v), so a
+// tile is a sum of outer products, C[(x, y)][(channel, z)] = sum over pairs of
+// A[(x, y)][p] B[p][(channel, z)] with A = wx wy (64 rows) and B = wz * value
+// (8 columns per channel): a GEMM with K = the item's pairs.  One warp runs it
+// with mma.sync m16n8k8 (TF32 in, FP32 accumulate), 8 pairs per K step, 4 x
+// NCH fragments of 16 x 8 held in registers.  TF32 keeps 11 significant bits,
+// so every operand is split into hi + lo TF32 parts and each K step issues
+// lo*hi, hi*lo and hi*hi (the lo*lo term is below 2^-22 relative), which
+// gives each product to about 2^-21.  Every 64 pairs the fragments are added
+// into per-lane double-float sums in shared memory and cleared, so the FP32
+// accumulation never carries more than 24 roundings.  Lane (g, t) owns the
+// cells x = g, z = 2t + {0, 1} and every y of the tile, both in the fragments
+// and in its sums, so the sums need no synchronisation.
+// The FP64 mass totals do not come from the cells: each pair adds
+// (sum wx)(sum wy)(sum wz), formed in double-float arithmetic, to its lane's
+// double-float total.
+constexpr int MMA_WARPS = 2;
+constexpr int MMA_FLUSH = 64;  // pairs between flushes of the fragments
+
+template <int NCH>
+struct MmaWarp {
+    float acc[NCH == 1 ? 2 : 9][16][32];  // [word][2 y + dz][lane]: n hi/lo, c hi/lo, halo hi/lo, v xyz
+    float w[32][WROW];                    // per pair of the chunk: wx[0..7] | wy[0..7] | wz[0..7]
+    float v[32][NCH == 1 ? 1 : 8];        // per pair: n, halo, c, vx, vy, vz values
+};
+
+__device__ __forceinline__ uint32_t tf32_rna(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+// x = hi + lo with hi, lo TF32 (hi carries x's 11 leading bits)
+__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo)
+{
+    hi = tf32_rna(x);
+    lo = tf32_rna(__fsub_rn(x, __uint_as_float(hi)));
+}
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// double-float (hi, lo) helpers in FP32 arithmetic: exact product of a
+// double-float and a float (two_prod by FMA), and accumulation
+__device__ __forceinline__ void df_mul(float& hi, float& lo, float b)
+{
+    const float p = __fmul_rn(hi, b);
+    const float e = fmaf(hi, b, -p);
+    hi = p;
+    lo = fmaf(lo, b, e);
+}
+__device__ __forceinline__ void df_mul_df(float& hi, float& lo, float bh, float bl)
+{
+    const float p = __fmul_rn(hi, bh);
+    const float e = fmaf(hi, bh, -p);
+    const float l = fmaf(hi, bl, fmaf(lo, bh, e));
+    const float s = __fadd_rn(p, l);
+    lo = __fsub_rn(l, __fsub_rn(s, p));
+    hi = s;
+}
+
+template <int NCH>
+__global__ void __launch_bounds__(32 * MMA_WARPS)
+k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
+              const uint32_t* __restrict__ item_off, const uint32_t* __restrict__ tstart,
+              const uint32_t* __restrict__ tcount, const uint32_t* __restrict__ pkeys,
+              const int* __restrict__ pvals, float* __restrict__ partial,
+              double* __restrict__ item_tot, int* __restrict__ next_item)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NW = NCH == 1 ? 2 : 9;
+    const int lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;
+    MmaWarp<NCH>& S = reinterpret_cast<MmaWarp<NCH>*>(smem_raw)[threadIdx.x >> 5];
+    const bool periodic = P.periodic != 0;
+    const uint32_t total_items = item_off[total_tiles];
+
+    for (;;) {
+        int item = 0, tile = -1;
+        if (lane == 0) {
+            item = atomicAdd(next_item, 1);
+            if ((uint32_t)item < total_items) tile = upper_index(item_off, total_tiles + 1, (uint32_t)item);
+        }
+        item = __shfl_sync(FULLM, item, 0);
+        tile = __shfl_sync(FULLM, tile, 0);
+        if ((uint32_t)item >= total_items) break;
+        const TileGeo geo = tile_geo(P, tile);
+        const MeshJob& J = P.job[geo.job];
+        const int nc = geo.nc;
+        const int seg = item - (int)item_off[tile];
+        const int nseg = (int)(item_off[tile + 1] - item_off[tile]);
+        const int j0 = (int)tstart[tile] + seg * P.seg;
+        const int j1 = (int)tstart[tile] + min((int)tcount[tile], (seg + 1) * P.seg);
+
+#pragma unroll
+        for (int k = 0; k < NW; ++k)
+#pragma unroll
+            for (int r = 0; r < 16; ++r) S.acc[k][r][lane] = 0.f;
+        float C[4][NCH][4];
+#pragma unroll
+        for (int mb = 0; mb < 4; ++mb)
+#pragma unroll
+            for (int ch = 0; ch < NCH; ++ch)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) C[mb][ch][i] = 0.f;
+        float tn_hi = 0.f, tn_lo = 0.f, th_hi = 0.f, th_lo = 0.f;  // this lane's pairs' totals
+
+        // adds the fragments into the lane's double-float sums and clears them
+        auto flush = [&]() {
+#pragma unroll
+            for (int mb = 0; mb < 4; ++mb)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int r = 2 * (2 * mb + (i >> 1)) + (i & 1);  // 2 y + dz
+                    float hi = S.acc[0][r][lane], lo = S.acc[1][r][lane];
+                    two_sum_acc(hi, lo, C[mb][0][i]);
+                    S.acc[0][r][lane] = hi;
+                    S.acc[1][r][lane] = lo;
+                    C[mb][0][i] = 0.f;
+                    if constexpr (NCH > 1) {
+                        hi = S.acc[4][r][lane]; lo = S.acc[5][r][lane];
+                        two_sum_acc(hi, lo, C[mb][1][i]);
+                        S.acc[4][r][lane] = hi; S.acc[5][r][lane] = lo;
+                        hi = S.acc[2][r][lane]; lo = S.acc[3][r][lane];
+                        two_sum_acc(hi, lo, C[mb][2][i]);
+                        S.acc[2][r][lane] = hi; S.acc[3][r][lane] = lo;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d)
+                            S.acc[6 + d][r][lane] = __fadd_rn(S.acc[6 + d][r][lane], C[mb][3 + d][i]);
+#pragma unroll
+                        for (int ch = 1; ch < NCH; ++ch) C[mb][ch][i] = 0.f;
+                    }
+                }
+        };
+
+        int since_flush = 0;
+        for (int c0 = j0; c0 < j1; c0 += 32) {
+            // ---- setup: one pair per lane: its image's cell range, 1-D weights
+            // (zero outside the range), channel values and FP64 mass ----
+            {
+                const int j = c0 + lane;
+                float* wl = S.w[lane];
+                float vals[NCH == 1 ? 1 : 6];
+#pragma unroll
+                for (int k = 0; k < (NCH == 1 ? 1 : 6); ++k) vals[k] = 0.f;
+#pragma unroll
+                for (int k = 0; k < 3 * TS; ++k) wl[k] = 0.f;
+                if (j < j1) {
+                    const int i = pvals[j];
+                    const int combo = (int)(pkeys[j] & ((1u << IMG_BITS) - 1u));
+                    const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
+                    const float4 A = rec[4 * (size_t)i];
+                    const float4 B = rec[4 * (size_t)i + 1];
+                    const float4 Cc = rec[4 * (size_t)i + 2];
+                    const float4 D = rec[4 * (size_t)i + 3];
+                    const float xs[3] = {A.x, A.y, A.z};
+                    const float lo[3] = {B.x, B.y, B.z};
+                    const float hi[3] = {Cc.x, Cc.y, Cc.z};
+                    const float hinv = A.w;
+                    float mh = 1.0f, ml = 0.0f;  // product of the three 1-D sums (double-float)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const AxisRange ar = axis_range(lo[a], hi[a], J, nc, periodic);
+                        const int k = ar.k_lo + dk[a];
+                        const int sh = k * nc + geo.O[a];
+                        const int r0 = max(ar.left - sh, 0), r1 = min(ar.right - sh, geo.E[a]);
+                        // cell t covers [fi*dx, (fi+1)*dx] with fi = t + sh (see k_deposit_items)
+                        float fi = (float)(r0 + sh);
+                        float e0 = __fmul_rn(__fmaf_rn(fi, J.dx, -xs[a]), hinv);
+                        float sh_ = 0.f, sl_ = 0.f;
+                        for (int c = r0; c < r1; ++c) {
+                            fi = __fadd_rn(fi, 1.0f);
+                            const float e1 = __fmul_rn(__fmaf_rn(fi, J.dx, -xs[a]), hinv);
+                            const float wv = tent_integral_rn(e0, e1);
+                            wl[a * TS + c] = wv;
+                            two_sum_acc(sh_, sl_, wv);
+                            e0 = e1;
+                        }
+                        if (a == 0) { mh = sh_; ml = sl_; }
+                        else df_mul_df(mh, ml, sh_, sl_);
+                    }
+                    const bool halo = (__float_as_int(D.z) & FLAG_HALO) != 0;
+                    if (!halo) {
+                        vals[0] = 1.0f;
+                        if constexpr (NCH > 1) {
+                            vals[2] = B.w;   // dens
+                            vals[3] = Cc.w;  // vx
+                            vals[4] = D.x;   // vy
+                            vals[5] = D.y;   // vz
+                        }
+                        two_sum_acc(tn_hi, tn_lo, mh);
+                        tn_lo = __fadd_rn(tn_lo, ml);
+                    } else {
+                        if constexpr (NCH > 1) vals[1] = 1.0f;
+                        two_sum_acc(th_hi, th_lo, mh);
+                        th_lo = __fadd_rn(th_lo, ml);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < (NCH == 1 ? 1 : 6); ++k) S.v[lane][k] = vals[k];
+            }
+            __syncwarp();
+            // ---- K steps of 8 pairs: pairs 8s + t (A) and 8s + t + 4 (B) for this lane ----
+            const int cnt = min(32, j1 - c0);
+            for (int s8 = 0; s8 < cnt; s8 += 8) {
+                const float* wa = S.w[s8 + t];
+                const float* wb = S.w[s8 + t + 4];
+                const float xa = wa[g], xb = wb[g];
+                const float za = wa[2 * TS + g], zb = wb[2 * TS + g];
+                uint32_t bh[NCH][2], bl[NCH][2];
+#pragma unroll
+                for (int ch = 0; ch < NCH; ++ch) {
+                    tf32_split(__fmul_rn(za, S.v[s8 + t][ch]), bh[ch][0], bl[ch][0]);
+                    tf32_split(__fmul_rn(zb, S.v[s8 + t + 4][ch]), bh[ch][1], bl[ch][1]);
+                }
+#pragma unroll
+                for (int mb = 0; mb < 4; ++mb) {
+                    uint32_t ah[4], al[4];
+                    tf32_split(__fmul_rn(xa, wa[TS + 2 * mb]), ah[0], al[0]);
+                    tf32_split(__fmul_rn(xa, wa[TS + 2 * mb + 1]), ah[1], al[1]);
+                    tf32_split(__fmul_rn(xb, wb[TS + 2 * mb]), ah[2], al[2]);
+                    tf32_split(__fmul_rn(xb, wb[TS + 2 * mb + 1]), ah[3], al[3]);
+#pragma unroll
+                    for (int ch = 0; ch < NCH; ++ch) {
+                        mma_tf32(C[mb][ch], al, bh[ch][0], bh[ch][1]);
+                        mma_tf32(C[mb][ch], ah, bl[ch][0], bl[ch][1]);
+                        mma_tf32(C[mb][ch], ah, bh[ch][0], bh[ch][1]);
+                    }
+                }
+            }
+            since_flush += 32;
+            if (since_flush >= MMA_FLUSH) {
+                flush();
+                since_flush = 0;
+            }
+            __syncwarp();  // the next chunk's setup overwrites S.w and S.v
+        }
+        if (since_flush > 0) flush();
+
+        // ---- this item's FP64 mass, then the tile (final) or the partial tile ----
+        double sn = (double)tn_hi + (double)tn_lo, shl = (double)th_hi + (double)th_lo;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sn += __shfl_down_sync(FULLM, sn, o);
+            shl += __shfl_down_sync(FULLM, shl, o);
+        }
+        if (nseg > 1) {
+            float* pt = partial + (size_t)item * TC * PW;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int y = r >> 1, z = 2 * t + (r & 1);
+                const int e = (z * TS + y) * TS + g;
+                pt[e] = S.acc[0][r][lane];
+                pt[TC + e] = S.acc[1][r][lane];
+                if constexpr (NCH > 1) {
+                    pt[2 * TC + e] = S.acc[2][r][lane];
+                    pt[3 * TC + e] = S.acc[3][r][lane];
+                    pt[4 * TC + e] = S.acc[6][r][lane];
+                    pt[5 * TC + e] = S.acc[7][r][lane];
+                    pt[6 * TC + e] = S.acc[8][r][lane];
+                    pt[7 * TC + e] = S.acc[4][r][lane];
+                    pt[8 * TC + e] = S.acc[5][r][lane];
+                }
+            }
+            if (lane == 0) {
+                item_tot[2 * item] = sn;
+                item_tot[2 * item + 1] = shl;
+            }
+        } else {
+            const size_t nmesh = (size_t)nc * nc * nc;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int y = r >> 1, z = 2 * t + (r & 1);
+                if (g >= geo.E[0] || y >= geo.E[1] || z >= geo.E[2]) continue;
+                const size_t idx = ((size_t)(geo.O[2] + z) * nc + (geo.O[1] + y)) * nc + (geo.O[0] + g);
+                J.mesh[idx] = __fadd_rn(S.acc[0][r][lane], S.acc[1][r][lane]);
+                if constexpr (NCH > 1) {
+                    J.mesh[nmesh + idx] = __fadd_rn(S.acc[4][r][lane], S.acc[5][r][lane]);
+                    J.mesh[2 * nmesh + idx] = __fadd_rn(S.acc[2][r][lane], S.acc[3][r][lane]);
+                    J.mesh[3 * nmesh + 3 * idx] = S.acc[6][r][lane];
+                    J.mesh[3 * nmesh + 3 * idx + 1] = S.acc[7][r][lane];
+                    J.mesh[3 * nmesh + 3 * idx + 2] = S.acc[8][r][lane];
+                }
+            }
+            if (lane == 0) {
+                J.partial[2 * geo.local] = sn;
+                J.partial[2 * geo.local + 1] = shl;
+            }
+        }
+        __syncwarp();  // the next item clears the sums
+    }
+}
+
+// ---------------------------------------------------------------------------
 // (5) merge the partial tiles of multi-segment tiles, in segment order
 // ---------------------------------------------------------------------------
+// item_tot (the tensor-core deposit): the FP64 mass of every item, summed in
+// item order; null: the mass is summed from the merged cells
 __global__ void __launch_bounds__(DEP_THREADS)
 k_merge_tiles(DepositParams P, int total_tiles, const uint32_t* __restrict__ item_off,
-              const float* __restrict__ partial)
+              const float* __restrict__ partial, const double* __restrict__ item_tot)
 {
     __shared__ double red[2][DEP_THREADS / 32];
     const int tile = blockIdx.x;
@@ -572,6 +879,18 @@ k_merge_tiles(DepositParams P, int total_tiles, const uint32_t* __restrict__ ite
             J.mesh[3 * nmesh + 3 * idx + 2] = vz;
         }
     }
+    if (item_tot) {
+        if (tid == 0) {
+            double a = 0.0, b = 0.0;
+            for (int it = i0; it < i1; ++it) {
+                a += item_tot[2 * it];
+                b += item_tot[2 * it + 1];
+            }
+            J.partial[2 * g.local] = a;
+            J.partial[2 * g.local + 1] = b;
+        }
+        return;
+    }
     block_totals(sn, sh, red, J, g.local, tid);
 }
 
@@ -592,6 +911,42 @@ static int key_bits(int total_tiles)
     int b = 0;
     while ((1 << b) < total_tiles) ++b;
     return b + IMG_BITS;
+}
+
+// ASG_DEPOSIT=simt selects the CUDA-core deposit (a comparison knob); the
+// default is the tensor-core one
+static bool use_mma_deposit()
+{
+    static const bool m = [] {
+        const char* e = std::getenv("ASG_DEPOSIT");
+        return !(e && std::strcmp(e, "simt") == 0);
+    }();
+    return m;
+}
+
+// per-item FP64 masses after the partial tiles of deposit_max_items items
+static double* deposit_item_totals(float* partial, uint32_t items)
+{
+    const size_t off = ((size_t)items * TC * PW * sizeof(float) + 15) & ~size_t(15);
+    return reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(partial) + off);
+}
+
+// a persistent kernel: as many CTAs as fit on every SM at once, its dynamic
+// shared memory allowed once per device (function attributes are per device)
+template <class... KArgs, class... Args>
+static void launch_persistent(void (*kern)(KArgs...), int dev, int sms, int threads, size_t smem,
+                              cudaStream_t s, Args... args)
+{
+    static std::atomic<unsigned long long> attr_set{0};  // one bit per device, per kernel
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_set.load() & bit)) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        attr_set.fetch_or(bit);
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    kern<<<sms * (per_sm > 0 ? per_sm : 1), threads, smem, s>>>(args...);
 }
 
 void launch_deposit_prep(const float4* pos, const float4* vel, const int* igrp, const float* rk,
@@ -631,22 +986,26 @@ void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t
     k_tile_items<<<(T + 1 + 255) / 256, 256, 0, s>>>(w.tstart, w.tcount, T, p.seg, w.item_off);
     exclusive_scan_u32(w.item_off, (size_t)T + 1, w.scan_tmp_t, s);
     cudaMemsetAsync(w.next_item, 0, sizeof(int), s);
-    const size_t smem = DEP_WARPS * sizeof(WarpTile);
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
-    static std::atomic<unsigned long long> attr_set{0};  // one bit per device (function attributes are per device)
-    const unsigned long long bit = 1ull << (dev & 63);
-    if (!(attr_set.load() & bit)) {
-        cudaFuncSetAttribute(k_deposit_items, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_deposit_items, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        attr_set.fetch_or(bit);
-    }
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_deposit_items, 32 * DEP_WARPS, smem);
-    const int grid = sms * (per_sm > 0 ? per_sm : 1);
-    k_deposit_items<<<grid, 32 * DEP_WARPS, smem, s>>>(w.rec, p, T, w.item_off, w.tstart, w.tcount,
-                                                       keys, vals, w.partial, w.next_item);
-    k_merge_tiles<<<T, DEP_THREADS, 0, s>>>(p, T, w.item_off, w.partial);
+    double* item_tot = nullptr;
+    if (use_mma_deposit()) {
+        item_tot = deposit_item_totals(w.partial, deposit_max_items(T, npairs, p.seg));
+        if (p.density_only)
+            launch_persistent(k_deposit_mma<1>, dev, sms, 32 * MMA_WARPS,
+                              MMA_WARPS * sizeof(MmaWarp<1>), s, w.rec, p, T, w.item_off, w.tstart,
+                              w.tcount, keys, vals, w.partial, item_tot, w.next_item);
+        else
+            launch_persistent(k_deposit_mma<6>, dev, sms, 32 * MMA_WARPS,
+                              MMA_WARPS * sizeof(MmaWarp<6>), s, w.rec, p, T, w.item_off, w.tstart,
+                              w.tcount, keys, vals, w.partial, item_tot, w.next_item);
+    } else {
+        launch_persistent(k_deposit_items, dev, sms, 32 * DEP_WARPS, DEP_WARPS * sizeof(WarpTile), s,
+                          w.rec, p, T, w.item_off, w.tstart, w.tcount, keys, vals, w.partial,
+                          w.next_item);
+    }
+    k_merge_tiles<<<T, DEP_THREADS, 0, s>>>(p, T, w.item_off, w.partial, item_tot);
     count_launches(3);
 }
 
@@ -657,7 +1016,11 @@ uint32_t deposit_max_items(int total_tiles, uint32_t npairs, int seg)
 
 int deposit_default_seg() { return SEG_DEFAULT; }
 
-size_t deposit_partial_bytes(uint32_t items) { return (size_t)items * TC * PW * sizeof(float); }
+// partial tiles of multi-item tiles, then each item's FP64 mass (2 doubles)
+size_t deposit_partial_bytes(uint32_t items)
+{
+    return (((size_t)items * TC * PW * sizeof(float) + 15) & ~size_t(15)) + 16 * (size_t)items;
+}
 
 __global__ void k_reduce_partials(const double* __restrict__ partial, int ntiles, double* out2)
 {

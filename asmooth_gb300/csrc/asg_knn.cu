@@ -308,12 +308,13 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
     if (want) idx33[base + lane] = result;
 }
 
-// dens is summed exactly, in any order, as 64-bit fixed point per receiver j:
-// a weight w is stored as w * 2^(FIX_BITS - e_j), where 2^e_j bounds
-// hinv_j^3.  A query q that has j in its 32-set has rk_j <= 2 rk_q (its 33
-// nearest lie within 2 rk_q of j), so w <= hinv_q^3 <= 8 hinv_j^3 and every
-// term stays below 2^(FIX_BITS + 3 + a rounding margin); the sum of a
-// receiver's terms is exact and independent of the order of the atomic adds.
+// dens is summed as 64-bit fixed point per receiver j: a weight w counts as
+// w * 2^(FIX_BITS - e_j), where 2^e_j bounds hinv_j^3.  A query q that has j in
+// its 32-set has rk_j <= 2 rk_q (its 33 nearest lie within 2 rk_q of j), so
+// w <= hinv_q^3 <= 8 hinv_j^3 and every term stays below 2^(FIX_BITS + 3 + a
+// rounding margin).  A lane adds one bucket's terms (at most 32, in query
+// order) as a double-float and converts the sum to an integer once; the
+// integer atomics make the total independent of the order of the buckets.
 constexpr int FIX_BITS = 40;
 
 // e_j with hinv_j^3 < 2^e_j (hinv^3 as the first factor of ker_rn); acc zeroed
@@ -372,7 +373,7 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
         const float4 c = pos[j];
         const float sc = __int_as_float((127 + FIX_BITS - dexp[j]) << 23);  // 2^(FIX_BITS - e_j)
         const int cj = __float_as_int(c.w);
-        unsigned long long sum = 0ull;
+        float sh = 0.0f, sl = 0.0f;  // sum of the scaled weights, double-float
         while (M) {
             const int k = __ffs(M) - 1;
             M &= M - 1;
@@ -386,9 +387,13 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
             w = __fmul_rn(w, __fsub_rn(1.0f, __fmul_rn(fabsf(dx), A.x)));
             w = __fmul_rn(w, __fsub_rn(1.0f, __fmul_rn(fabsf(dy), A.x)));
             w = __fmul_rn(w, __fsub_rn(1.0f, __fmul_rn(fabsf(dz), A.x)));
-            if (member) sum += __float2ull_rn(__fmul_rn(w, sc));
+            // w * 2^(FIX_BITS - e_j) is exact (a power-of-two scale)
+            if (member) two_sum_acc_nonneg(sh, sl, __fmul_rn(w, sc));
         }
-        if (have && sum) atomicAdd(&acc[j], sum);
+        // one conversion per receiver and bucket: hi and lo rounded to integers
+        // (lo may be negative; the sum is not)
+        const long long sum = __float2ll_rn(sh) + __float2ll_rn(sl);
+        if (have && sum) atomicAdd(&acc[j], (unsigned long long)sum);
     };
     // the queries whose radius reaches a bucket node's box
     auto reach = [&](int node) -> unsigned {

@@ -522,10 +522,10 @@ static int dep_range(const float* y, float h, float boxsize, int nc, int periodi
  * its contributions in the serial loop's order and the float mesh is the
  * serial one bit for bit.  The FP64 totals are summed per plane, then over
  * the planes in order.  mesh64 holds the FP64 restatement (weights computed in
- * double), or with fw the FP64 sums of the library's float weights
- * (lib_weight: ker3 = (k0*k1)*k2, ker3*dens and ker3*v, products exact in
- * double).  The totals are always the FP64 sums of the library's float
- * weights (n and halo), the quantity the library's FP64 totals reproduce.
+ * double), or with fw the FP64 sums of the library's cell weights: the
+ * products k0*k1*k2 of its float 1-D weights (lib_weight) taken in double,
+ * times 1, dens or v.  The totals are always the FP64 sums of those weights (n
+ * and halo), the quantity the library's FP64 totals reproduce.
  * Returns -4 if some rk is not positive. */
 static int dep_by_planes(const float* x, const float* v, const float* dens, const float* rk,
                          const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
@@ -601,21 +601,22 @@ static int dep_by_planes(const float* x, const float* v, const float* dens, cons
                     const size_t idx = (size_t)p * nc2 + (size_t)((iy % nc + nc) % nc) * nc +
                                        (size_t)((ix % nc + nc) % nc);
                     const float ker3 = k0 * k1 * k2;
-                    const float lw3 = lw ? lib_weight(ix, dx, xp[0], hinv) * l1 * l2 : 0.0f;
+                    const double lw3 = lw ? (double)lib_weight(ix, dx, xp[0], hinv) * (double)l1 *
+                                                (double)l2 : 0.0;
                     if (!to_halo) {
                         mn[idx] += ker3;
                         mc[idx] += ker3 * dens[j];
                         mv[3 * idx] += ker3 * v[3 * (size_t)j];
                         mv[3 * idx + 1] += ker3 * v[3 * (size_t)j + 1];
                         mv[3 * idx + 2] += ker3 * v[3 * (size_t)j + 2];
-                        tn += (double)lw3;
+                        tn += lw3;
                     } else {
                         mh[idx] += ker3;
-                        th += (double)lw3;
+                        th += lw3;
                     }
                     if (mesh64) {
                         t64 = ((double)ix * (double)dx - (double)xp[0]) * hinv64;
-                        const double w = fw ? (double)lw3 : ker_integ64(t64, t64 + ds64) * k1d * k2d;
+                        const double w = fw ? lw3 : ker_integ64(t64, t64 + ds64) * k1d * k2d;
                         if (!to_halo) {
                             mesh64[idx] += w;
                             mesh64[2 * nmesh + idx] += w * (double)dens[j];
@@ -782,9 +783,9 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
 }
 
 /* As orc_assign_on_mesh (float mesh the same bit for bit), with mesh64 and the
- * totals the FP64 sums of the library's float weights (lib_weight) instead of
- * the FP64 restatement: what a deposit that sums those weights without
- * rounding error gives. */
+ * totals the FP64 sums of the library's cell weights (the products of its
+ * float 1-D weights, lib_weight) instead of the FP64 restatement: what a
+ * deposit that forms and sums those weights without rounding error gives. */
 int orc_assign_on_mesh_fw(const float* x, const float* v, const float* dens, const float* rk,
                           const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
                           const float* offset, int nthreads, float* mesh, double* mesh64,

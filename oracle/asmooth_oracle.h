@@ -58,8 +58,9 @@ int orc_dens_from_lists(const float* x, int n, const int* nbr, const float* t33,
  * cube offset, 3 floats).  mesh (6*nc^3 floats, reference layout
  * [n | halo | c | v xyz interleaved]) is ADDED to (clear it first).
  * mesh64 (optional, 6*nc^3 doubles): the same cells with FP64 weights.
- * totals (optional, 2 doubles): FP64 sums of the library's float weights (its
- * more accurate cell integrals, lib_weight) deposited into n and into halo.
+ * totals (optional, 2 doubles): FP64 sums of the library's cell weights (the
+ * products of its float 1-D cell integrals, lib_weight) deposited into n and
+ * into halo.
  * With mesh64 or totals the work runs over mesh planes in parallel (the float
  * mesh stays the serial loop's bit for bit); otherwise nthreads > 1 runs the
  * reference's OpenMP loop with atomics (timing only). */
@@ -69,7 +70,7 @@ int orc_assign_on_mesh(const float* x, const float* v, const float* dens, const 
                        float* mesh, double* mesh64, double* totals);
 
 /* n-channel-only variant (coarse_mesh.cpp:212-269). mesh has nc^3 floats. */
-/* as orc_assign_on_mesh; mesh64, totals = FP64 sums of the library's float weights */
+/* as orc_assign_on_mesh; mesh64, totals = FP64 sums of the library's cell weights */
 int orc_assign_on_mesh_fw(const float* x, const float* v, const float* dens, const float* rk,
                           const int* igrp, int n, float boxsize, int nc, int sign, int periodic,
                           const float* offset, int nthreads, float* mesh, double* mesh64,

@@ -104,8 +104,9 @@ class Oracle:
                        offset=(0.0, 0.0, 0.0), nthreads=1, want64=True, float_weights=False):
         """(float mesh, FP64 mesh, FP64 totals).  The float mesh is the
         reference's; the FP64 mesh is the FP64 restatement, or with
-        float_weights the FP64 sums of the library's float weights (its more
-        accurate evaluation of the tent integrals: ker3, ker3*dens, ker3*v)."""
+        float_weights the FP64 sums of the library's cell weights (the
+        products of its float 1-D cell integrals, times 1, dens, v).  The
+        totals are the FP64 sums of the library's cell weights."""
         x = np.ascontiguousarray(x, np.float32)
         n = x.shape[0]
         mesh = np.zeros(6 * nc ** 3, np.float32)

@@ -51,6 +51,12 @@ def rel_err_cells(got: np.ndarray, ref: np.ndarray, weight: np.ndarray, frac: fl
     return float(np.max(np.abs(got[sel].astype(np.float64) - ref[sel]) / np.abs(ref[sel])))
 
 
+# The deposit's per-cell error against the FP64 sums of its own cell weights
+# (products of its float 1-D weights): 3xTF32 tensor-core products (at most
+# 2^-21 relative) plus at most 24 FP32 accumulator roundings (2^-23 each)
+# between two flushes into double-float sums.
+DEP_TOL = 4e-6
+
 # adversarial deposit inputs: a box of side EDGE_L meshed at EDGE_NCS (cells of 4
 # and 2 units, 8-cell tiles of 32 and 16 units)
 EDGE_L = 64.0

@@ -4,33 +4,30 @@ box faces (clipping), halo and non-halo particles under both signs, in the
 plain (coarse_mesh.cpp:45-127), periodic (global_mesh.cpp:25-123) and
 density-only (coarse_mesh.cpp:212-269) deposits.
 
-The library evaluates each cell's tent integral more accurately than the
+The library evaluates each cell's 1-D tent integral more accurately than the
 reference's float ker_integ (coarse_mesh.cpp:10-22, 80-90): cell edges as
-fma(i, dx, -x) * hinv and cancellation-free forms of the integral.  The oracle
-restates those float operations in C (lib_weight).  Three checks, all through
-the C ABI:
+fma(i, dx, -x) * hinv and cancellation-free forms of the integral; a cell's
+weight is the product of the three, formed on the tensor cores.  The oracle
+restates the 1-D weights in C (lib_weight) and sums the products in FP64.
+Three checks, all through the C ABI:
   * disjoint supports: the particles are split into batches whose cell boxes
-    do not overlap, so every cell receives at most one weight; every channel
-    then equals the oracle's restatement bit for bit (ker3, ker3*dens, ker3*v
-    each correctly rounded);
-  * the whole set at once: n, c and halo are the correctly rounded FP64 sums of
-    those float weights (error at most 2^-24 relative plus the double-float
-    accumulation's 2^-38), v within 1e-5 of |v| + n, and the FP64 mass totals
-    within 1e-12 of the FP64 sums of the float weights;
+    do not overlap, so every cell receives at most one weight, which must match
+    the oracle's to DEP_TOL relative in n, c and halo, v within DEP_TOL of
+    |v| + n;
+  * the whole set at once: the same bars on every cell, and the FP64 mass
+    totals within 1e-12 of the FP64 sums of the weights;
   * accuracy: every channel within 1e-5 of the FP64 restatement (cells above
     1e-3 of the mean density), the bar the reference's own float weights miss
     on these inputs."""
 import numpy as np
 import pytest
 
-from helpers import EDGE_L as L, EDGE_NCS as NCS, edge_inputs, field_errors
+from helpers import DEP_TOL, EDGE_L as L, EDGE_NCS as NCS, edge_inputs, field_errors
 
 from asmooth_gb300 import api
 
 pytestmark = pytest.mark.gpu
 
-ROUND_TOL = 2.0 ** -24 + 2.0 ** -38
-V_TOL = 1e-5
 TOTAL_TOL = 1e-12
 FIELD_TOL = 1e-5
 
@@ -103,28 +100,24 @@ def test_deposit_edges(gpu_ctx, oracle, mode, sign, nc):
         x, v, dens, rk, igrp = x[inside], v[inside], dens[inside], rk[inside], igrp[inside]
     nm = nc ** 3
 
-    # one weight per cell: bit for bit the oracle's restatement of the float weights
+    # one weight per cell, then the whole set: the oracle's FP64 sums of the
+    # library's cell weights to DEP_TOL
     batches = disjoint_batches(x, rk, nc, mode == "periodic")
     assert len(batches) < len(x)  # the batches do combine particles
-    for b in batches:
+    for b in batches + [np.arange(len(x))]:
         b = np.asarray(b)
-        got, _ = gpu_mesh(gpu_ctx, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
-        s64, _ = oracle_mesh(oracle, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
-        assert np.array_equal(bits(got), bits(s64.astype(np.float32))), (mode, sign, nc, b[:4])
-
-    # the whole set: correctly rounded FP64 sums of the float weights
-    got, tot = gpu_mesh(gpu_ctx, mode, x, v, dens, rk, igrp, nc, sign)
-    s64, t64 = oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign)
-    chans = [(0, nm)] if mode == "density" else [(0, nm), (nm, 2 * nm), (2 * nm, 3 * nm)]
-    for a, e in chans:
-        g, s = got[a:e].astype(np.float64), s64[a:e]
-        assert np.all(np.abs(g - s) <= ROUND_TOL * np.abs(s) + 1e-300), (mode, sign, nc, a)
-    if mode != "density":
-        vs = s64[3 * nm:]
-        scale = np.abs(vs) + np.repeat(s64[:nm], 3)
-        assert np.all(np.abs(got[3 * nm:].astype(np.float64) - vs) <= V_TOL * scale + 1e-30)
-        for k in range(2):
-            assert abs(tot[k] - t64[k]) <= TOTAL_TOL * max(abs(t64[k]), 1e-300), (k, tot, t64)
+        got, tot = gpu_mesh(gpu_ctx, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
+        s64, t64 = oracle_mesh(oracle, mode, x[b], v[b], dens[b], rk[b], igrp[b], nc, sign)
+        chans = [(0, nm)] if mode == "density" else [(0, nm), (nm, 2 * nm), (2 * nm, 3 * nm)]
+        for a, e in chans:
+            g, s = got[a:e].astype(np.float64), s64[a:e]
+            assert np.all(np.abs(g - s) <= DEP_TOL * np.abs(s)), (mode, sign, nc, a, b[:4])
+        if mode != "density":
+            vs = s64[3 * nm:]
+            scale = np.abs(vs) + np.repeat(s64[:nm], 3)
+            assert np.all(np.abs(got[3 * nm:].astype(np.float64) - vs) <= DEP_TOL * scale)
+            for k in range(2):
+                assert abs(tot[k] - t64[k]) <= TOTAL_TOL * abs(t64[k]), (k, tot, t64)
 
     # accuracy against the FP64 restatement of the weights
     e64, _ = oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign, float_weights=False)

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import pyoracle as po
-from helpers import dens_brute, exact_t33, rel_err_cells, set_from_key
+from helpers import DEP_TOL, dens_brute, exact_t33, rel_err_cells, set_from_key
 
 from asmooth_gb300 import api
 from asmooth_gb300 import synthetic as syn
@@ -218,9 +218,9 @@ def test_smooth_pipeline_matches_staged_calls(gpu_ctx):
     gpu_ctx.mark_halo_particles(p3, halos, cube.left, cube.right)
     m3, t3 = gpu_ctx.assign_on_meshes(p3, cube.boxsize, ncs, sign=-1)
     assert p1.tobytes() == p3.tobytes()
-    for a, b, nc in zip(m1, m3, ncs):
+    for a, b, nc in zip(m1, m3, ncs):  # each within DEP_TOL of the same FP64 sums
         n = a[: nc ** 3]
-        assert rel_err_cells(b[: nc ** 3], n.astype(np.float64), n) <= 1e-6
+        assert rel_err_cells(b[: nc ** 3], n.astype(np.float64), n) <= 2 * DEP_TOL
     assert np.allclose(t1, t3, rtol=1e-12, atol=0)
 
 

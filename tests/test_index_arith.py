@@ -21,14 +21,16 @@ def test_deposit_reciprocal_division():
 
 
 def test_dens_fixed_point_sums():
-    """k_dens_scatter adds 64-bit fixed-point terms w * 2^(FIX_BITS - e_j), each
-    below 2^(FIX_BITS + 4) (w <= 8 hinv_j^3 < 2^(e_j + 3), one rounding), in a
-    lane register over at most the 32 queries of a bundle per bucket, then into
-    acc[j] with one atomic: neither the register nor acc can overflow before a
-    receiver collects 2^(60 - FIX_BITS) terms."""
+    """k_dens_scatter counts a weight w as w * 2^(FIX_BITS - e_j), below
+    2^(FIX_BITS + 4) (w <= 8 hinv_j^3 < 2^(e_j + 3), one rounding); a lane sums
+    at most the 32 queries of a bundle per bucket as a double-float, rounds hi
+    and lo to integers and adds them to acc[j] with one atomic: neither the
+    per-bucket sum nor acc can overflow before a receiver collects
+    2^(60 - FIX_BITS) terms."""
     src = open(os.path.join(CSRC, "asg_knn.cu")).read()
     fix = int(re.search(r"constexpr int FIX_BITS = (\d+);", src).group(1))
-    assert "sum += __float2ull_rn(__fmul_rn(w, sc));" in src
+    assert "two_sum_acc_nonneg(sh, sl, __fmul_rn(w, sc));" in src
+    assert "__float2ll_rn(sh) + __float2ll_rn(sl)" in src
     term = 2 ** (fix + 4)
-    assert 32 * term < 2 ** 64
+    assert 32 * term < 2 ** 63
     assert 2 ** (60 - fix) * term <= 2 ** 64 and 2 ** (60 - fix) >= 2 ** 20
