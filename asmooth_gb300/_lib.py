@@ -49,6 +49,7 @@ SIGNATURES = {
     "asg_batch_destroy": (None, [_vp]),
     "asg_batch_set_item": (_i, [_vp, _i, _vp, _vp, _i]),
     "asg_batch_tune": (_i, [_vp, _ip, _ip]),
+    "asg_batch_config": (_i, [_vp, _ip, _ip, _ip, _ip]),
     "asg_batch_set_streams": (_i, [_vp, _i]),
     "asg_batch_run": (_i, [_vp]),
     "asg_batch_stats": (_i, [_vp, _dp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),

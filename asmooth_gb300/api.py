@@ -507,6 +507,13 @@ class Batch:
         self.ctx._ok(self.lib.asg_batch_tune(self.h, C.byref(leaf), C.byref(seg)))
         return leaf.value, seg.value
 
+    def config(self) -> dict:
+        """The configuration the batch runs with (tuned or default)."""
+        v = [C.c_int(0) for _ in range(4)]
+        self.ctx._ok(self.lib.asg_batch_config(self.h, *[C.byref(x) for x in v]))
+        return {"leaf": v[0].value, "seg": v[1].value, "knn_warps": v[2].value,
+                "tensor_deposit": bool(v[3].value)}
+
     def run(self):
         self.ctx._ok(self.lib.asg_batch_run(self.h))
 

@@ -59,6 +59,8 @@ struct asg_ctx {
     bool loaded = false, knn_done = false, rk_checked = false, idx33_all = false;
     int leaf = 32;  // tree bucket size scanned whole by the traversals (fastest on GB300)
     int dep_seg = 4096;  // pairs per deposit work item
+    int knn_warps = 2;   // warps per block of the neighbour search (2 or 4)
+    int dep_mma = deposit_default_mma();  // deposit on the tensor cores (1) or CUDA cores (0)
     int* perm = nullptr;       // sorted position -> input index
     uint64_t* keys = nullptr;  // sorted keys
 
@@ -891,7 +893,7 @@ static int run_knn(asg_ctx* ctx)
     const TreeView t = tree_view(ctx);
     phase_begin(ctx, ASG_PH_KNN);
     launch_knn_t33(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<float>(ctx->rk),
-                   P<int>(ctx->idx33), P<int>(ctx->blist), ctx->d_err, ctx->s);
+                   P<int>(ctx->idx33), P<int>(ctx->blist), ctx->d_err, ctx->s, ctx->knn_warps);
     phase_end(ctx);
     phase_begin(ctx, ASG_PH_TIES);  // only bundles with an exact tie at the 33rd distance
     launch_knn_ties(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33), 0,
@@ -1056,6 +1058,7 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     p.periodic = periodic ? 1 : 0;
     p.density_only = density_only ? 1 : 0;
     p.seg = ctx->dep_seg;
+    p.mma = ctx->dep_mma;
     for (int d = 0; d < 3; ++d) p.offset[d] = periodic && coords ? boxsize * (float)coords[d] : 0.0f;
     int tiles = 0;
     for (int k = 0; k < n_nc; ++k) {
@@ -1654,6 +1657,8 @@ int batch_plan(asg_batch* b)
     for (asg_ctx* c : b->sub) {
         c->leaf = ctx->leaf;  // the tuned configuration applies to every stream
         c->dep_seg = ctx->dep_seg;
+        c->knn_warps = ctx->knn_warps;
+        c->dep_mma = ctx->dep_mma;
         if (int r = alloc_set(c, b->max_n)) return fail(ctx, r, "batch: stream scratch");
         if (int r = grow(c, c->lab_scan, 4 * (size_t)b->max_n)) return fail(ctx, r, "batch: stream scratch");
     }
@@ -1857,33 +1862,54 @@ int asg_batch_tune(asg_batch* b, int* leaf, int* seg)
     int item = 0;  // the largest item
     for (int i = 1; i < b->n_items; ++i)
         if (b->np[(size_t)i] > b->np[(size_t)item]) item = i;
-    const int leaves[] = {16, 24, 32}, segs[] = {2048, 4096, 8192};
+    // tree bucket size x deposit work-item length x neighbour-search warps per
+    // block x deposit engine (tensor cores or CUDA cores)
+    const int leaves[] = {16, 24, 32}, segs[] = {2048, 4096, 8192}, warps[] = {2, 4}, mmas[] = {1, 0};
     float best = INFINITY;
-    int bl = ctx->leaf, bs = ctx->dep_seg;
+    int bl = ctx->leaf, bs = ctx->dep_seg, bw = ctx->knn_warps, bm = ctx->dep_mma;
     for (int l : leaves)
-        for (int s : segs) {
-            ctx->leaf = l;
-            ctx->dep_seg = s;
-            float ms = 0.0f;
-            for (int rep = 0; rep < 2; ++rep) {  // the first repetition warms up
-                CK(cudaEventRecord(b->e0, ctx->s));
-                if (int r = batch_queue_item(b, ctx, item, 0)) return r;
-                CK(cudaEventRecord(b->e1, ctx->s));
-                CK(cudaEventSynchronize(b->e1));
-                CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
-            }
-            if (ms < best) {
-                best = ms;
-                bl = l;
-                bs = s;
-            }
-        }
+        for (int sg : segs)
+            for (int w : warps)
+                for (int m : mmas) {
+                    ctx->leaf = l;
+                    ctx->dep_seg = sg;
+                    ctx->knn_warps = w;
+                    ctx->dep_mma = m;
+                    float ms = 0.0f;
+                    for (int rep = 0; rep < 2; ++rep) {  // the first repetition warms up
+                        CK(cudaEventRecord(b->e0, ctx->s));
+                        if (int r = batch_queue_item(b, ctx, item, 0)) return r;
+                        CK(cudaEventRecord(b->e1, ctx->s));
+                        CK(cudaEventSynchronize(b->e1));
+                        CK(cudaEventElapsedTime(&ms, b->e0, b->e1));
+                    }
+                    if (ms < best) {
+                        best = ms;
+                        bl = l;
+                        bs = sg;
+                        bw = w;
+                        bm = m;
+                    }
+                }
     ctx->leaf = bl;
     ctx->dep_seg = bs;
+    ctx->knn_warps = bw;
+    ctx->dep_mma = bm;
     batch_drop_graph(b);  // a new configuration needs a new plan and capture
     if (leaf) *leaf = bl;
     if (seg) *seg = bs;
     return finish(ctx, "batch tune");
+}
+
+int asg_batch_config(asg_batch* b, int* leaf, int* seg, int* knn_warps, int* tensor_deposit)
+{
+    if (!b) return ASG_ERR_ARG;
+    const asg_ctx* ctx = b->ctx;
+    if (leaf) *leaf = ctx->leaf;
+    if (seg) *seg = ctx->dep_seg;
+    if (knn_warps) *knn_warps = ctx->knn_warps;
+    if (tensor_deposit) *tensor_deposit = ctx->dep_mma;
+    return ASG_OK;
 }
 
 int asg_batch_run(asg_batch* b)

@@ -547,9 +547,12 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
 // and in its sums, so the sums need no synchronisation.
 // The FP64 mass totals do not come from the cells: each pair adds
 // (sum wx)(sum wy)(sum wz), formed in double-float arithmetic, to its lane's
-// double-float total.
+// double-float total.  A K step skips the row blocks (two y rows each) and the
+// channels that none of its 8 pairs touches: their products are exact zeros.
 constexpr int MMA_WARPS = 2;
 constexpr int MMA_FLUSH = 64;  // pairs between flushes of the fragments
+constexpr uint32_t INFO_MAIN = 1u << 8;  // a pair deposits into n, c and v
+constexpr uint32_t INFO_HALO = 1u << 9;  // a pair deposits into halo
 
 template <int NCH>
 struct MmaWarp {
@@ -676,7 +679,10 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
         int since_flush = 0;
         for (int c0 = j0; c0 < j1; c0 += 32) {
             // ---- setup: one pair per lane: its image's cell range, 1-D weights
-            // (zero outside the range), channel values and FP64 mass ----
+            // (zero outside the range), channel values and FP64 mass; info =
+            // the y rows it touches (bits 0-7) and whether it deposits into the
+            // n, c, v channels (INFO_MAIN) or the halo channel (INFO_HALO) ----
+            uint32_t info = 0;
             {
                 const int j = c0 + lane;
                 float* wl = S.w[lane];
@@ -718,8 +724,10 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                         }
                         if (a == 0) { mh = sh_; ml = sl_; }
                         else df_mul_df(mh, ml, sh_, sl_);
+                        if (a == 1 && r1 > r0) info = ((1u << r1) - 1u) & ~((1u << r0) - 1u);
                     }
                     const bool halo = (__float_as_int(D.z) & FLAG_HALO) != 0;
+                    if (info) info |= halo ? INFO_HALO : INFO_MAIN;
                     if (!halo) {
                         vals[0] = 1.0f;
                         if constexpr (NCH > 1) {
@@ -743,6 +751,10 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
             // ---- K steps of 8 pairs: pairs 8s + t (A) and 8s + t + 4 (B) for this lane ----
             const int cnt = min(32, j1 - c0);
             for (int s8 = 0; s8 < cnt; s8 += 8) {
+                // the rows and channels the step's 8 pairs touch (warp-uniform);
+                // the products of the others are exact zeros and are skipped
+                const uint32_t kinfo =
+                    __reduce_or_sync(FULLM, (lane >= s8 && lane < s8 + 8) ? info : 0u);
                 const float* wa = S.w[s8 + t];
                 const float* wb = S.w[s8 + t + 4];
                 const float xa = wa[g], xb = wb[g];
@@ -750,11 +762,13 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                 uint32_t bh[NCH][2], bl[NCH][2];
 #pragma unroll
                 for (int ch = 0; ch < NCH; ++ch) {
+                    if (!(kinfo & (ch == 1 && NCH > 1 ? INFO_HALO : INFO_MAIN))) continue;
                     tf32_split(__fmul_rn(za, S.v[s8 + t][ch]), bh[ch][0], bl[ch][0]);
                     tf32_split(__fmul_rn(zb, S.v[s8 + t + 4][ch]), bh[ch][1], bl[ch][1]);
                 }
 #pragma unroll
                 for (int mb = 0; mb < 4; ++mb) {
+                    if (!(kinfo & (3u << (2 * mb)))) continue;
                     uint32_t ah[4], al[4];
                     tf32_split(__fmul_rn(xa, wa[TS + 2 * mb]), ah[0], al[0]);
                     tf32_split(__fmul_rn(xa, wa[TS + 2 * mb + 1]), ah[1], al[1]);
@@ -762,6 +776,7 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                     tf32_split(__fmul_rn(xb, wb[TS + 2 * mb + 1]), ah[3], al[3]);
 #pragma unroll
                     for (int ch = 0; ch < NCH; ++ch) {
+                        if (!(kinfo & (ch == 1 && NCH > 1 ? INFO_HALO : INFO_MAIN))) continue;
                         mma_tf32(C[mb][ch], al, bh[ch][0], bh[ch][1]);
                         mma_tf32(C[mb][ch], ah, bl[ch][0], bl[ch][1]);
                         mma_tf32(C[mb][ch], ah, bh[ch][0], bh[ch][1]);
@@ -913,13 +928,13 @@ static int key_bits(int total_tiles)
     return b + IMG_BITS;
 }
 
-// ASG_DEPOSIT=simt selects the CUDA-core deposit (a comparison knob); the
-// default is the tensor-core one
-static bool use_mma_deposit()
+// the default deposit engine: the tensor cores, or the CUDA cores with
+// ASG_DEPOSIT=simt (a comparison knob; a context's tuner may choose either)
+int deposit_default_mma()
 {
-    static const bool m = [] {
+    static const int m = [] {
         const char* e = std::getenv("ASG_DEPOSIT");
-        return !(e && std::strcmp(e, "simt") == 0);
+        return (e && std::strcmp(e, "simt") == 0) ? 0 : 1;
     }();
     return m;
 }
@@ -990,7 +1005,7 @@ void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     double* item_tot = nullptr;
-    if (use_mma_deposit()) {
+    if (p.mma) {
         item_tot = deposit_item_totals(w.partial, deposit_max_items(T, npairs, p.seg));
         if (p.density_only)
             launch_persistent(k_deposit_mma<1>, dev, sms, 32 * MMA_WARPS,

@@ -88,9 +88,10 @@ void exclusive_scan_u32(uint32_t* data, size_t n, void* temp, cudaStream_t s);
 constexpr int KNN_LIST = 96;
 inline size_t knn_list_words(int n) { return (size_t)((n + 31) / 32) * (KNN_LIST + 1); }
 // t33, rk = sqrtf(t33), idx33 = -1 (no tie at the 33rd) or -2 (ties to resolve);
-// blist (knn_list_words ints, or null) receives the scanned buckets
+// blist (knn_list_words ints, or null) receives the scanned buckets; warps: 2 or
+// 4 warps per block (tuning)
 void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, float* rk, int* idx33,
-                    int* blist, int* err, cudaStream_t s);
+                    int* blist, int* err, cudaStream_t s, int warps = 2);
 // idx33 = input index of the 33rd key, for flagged queries (all = 0) or every query
 void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int* idx33,
                      int all, int* err, cudaStream_t s);
@@ -120,6 +121,7 @@ struct DepositParams {
     float offset[3];  // periodic: rank cube offset
     int density_only;
     int seg;          // pairs per work item of the persistent deposit (tuning, > 0)
+    int mma;          // 1: the tensor-core deposit, 0: the CUDA-core one (tuning)
 };
 // scratch of one deposit: particle records, (tile, image) pairs, work items
 struct DepositScratch {
@@ -142,6 +144,7 @@ size_t deposit_prep_bytes(int n);
 size_t deposit_tile_bytes(int total_tiles);
 uint32_t deposit_max_items(int total_tiles, uint32_t npairs, int seg);
 int deposit_default_seg();
+int deposit_default_mma();
 size_t deposit_partial_bytes(uint32_t items);
 // pass 1: particle records and pair counts; pcount[n] then holds the number of pairs
 void launch_deposit_prep(const float4* pos, const float4* vel, const int* igrp, const float* rk,

@@ -31,10 +31,10 @@
 namespace asg {
 
 constexpr int KNN_WARPS = 4;
-// k_knn_t33 runs in blocks of 2 warps, 16 per SM at 64 registers: a warp that
-// finishes early frees its slot sooner than in a block of 4 (23.07 against
-// 23.25 ms on the 256^3 step)
-constexpr int T33_WARPS = 2;
+// k_knn_t33 runs in blocks of W = 2 or 4 warps (32 warps per SM at 64
+// registers either way); in blocks of 2 a warp that finishes early frees its
+// slot sooner (23.07 against 23.25 ms on the 256^3 step in Morton order).  The
+// batched form's autotuner picks W.
 constexpr unsigned FULL = 0xffffffffu;
 
 // Merges a lane's queued candidates (KNN_QUEUE values in shared memory, column
@@ -81,7 +81,8 @@ __device__ __forceinline__ float child_dist2(const float4* __restrict__ pos, con
 // each candidate as it comes.  Thresholds are the merged a[32], an upper bound
 // of the true one while values wait in the queue.  The ids of the buckets
 // scanned go to blist for k_dens_scatter.
-__global__ void __launch_bounds__(T33_WARPS * 32, 16)
+template <int T33_WARPS>
+__global__ void __launch_bounds__(T33_WARPS * 32, 32 / T33_WARPS)
 k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
           float* __restrict__ rk, int* __restrict__ idx33, int* __restrict__ blist, int* err)
 {
@@ -480,11 +481,13 @@ __global__ void k_dens_finish(const unsigned long long* __restrict__ acc,
 static int knn_blocks(int n) { return (n + KNN_WARPS * 32 - 1) / (KNN_WARPS * 32); }
 
 void launch_knn_t33(const float4* pos, const TreeView& t, float* t33, float* rk, int* idx33,
-                    int* blist, int* err, cudaStream_t s)
+                    int* blist, int* err, cudaStream_t s, int warps)
 {
     if (t.n <= 0) return;
-    k_knn_t33<<<(t.n + T33_WARPS * 32 - 1) / (T33_WARPS * 32), T33_WARPS * 32, 0, s>>>(
-        pos, t, t33, rk, idx33, blist, err);
+    if (warps == 4)
+        k_knn_t33<4><<<(t.n + 127) / 128, 128, 0, s>>>(pos, t, t33, rk, idx33, blist, err);
+    else
+        k_knn_t33<2><<<(t.n + 63) / 64, 64, 0, s>>>(pos, t, t33, rk, idx33, blist, err);
     count_launches(1);
 }
 

@@ -278,25 +278,42 @@ WORKLOADS = {
 }
 
 
+def _batch_cube(n, box, cseed, f, n_halos, contractions):
+    """One cube of the batched workload at every contraction (a pool task)."""
+    out = []
+    for con in contractions:
+        x, v = nfw_cube(n, box, cseed, frac_halo=f, n_halos=n_halos, halo_contraction=con)
+        out.append(add_periodic_shell(x, v, box, 8.0))
+    return out
+
+
 def make_batch(seed: int = 4, scale: int = 1, n_cubes: int = 27,
-               contractions=(1.0, 0.7, 0.5)) -> tuple[list, tuple]:
+               contractions=(1.0, 0.7, 0.5), workers: int = 1) -> tuple[list, tuple]:
     """The batched workload: ``n_cubes`` node-cubes of side 256 (mean
     separation 2, so 128^3 particles on average), each with its own halo
     fraction f ~ U[0.2, 0.8] and a particle count 128^3 * (1 + (f - 0.5)/2)
     that varies with it, NFW halos as in the 256^3 cube (625 per cube), and
     one item per redshift with every halo contracted by the given factor about
-    its centre.  Items are ordered cube-major; nc = 32, 64, 128."""
+    its centre.  Items are ordered cube-major; nc = 32, 64, 128.  workers > 1
+    generates the cubes in a process pool (started with spawn, so it is safe
+    after CUDA has been initialised); the items do not depend on it."""
     rng = np.random.default_rng(seed)
     box = 256.0 / scale
     npd = 128 // scale
-    items = []
+    tasks = []
     for c in range(n_cubes):
         f = float(rng.uniform(0.2, 0.8))
         n = int(round(npd ** 3 * (1.0 + 0.5 * (f - 0.5))))
-        for con in contractions:
-            x, v = nfw_cube(n, box, 1000 * seed + c, frac_halo=f, n_halos=max(8, 625 // scale ** 3),
-                            halo_contraction=con)
-            items.append(add_periodic_shell(x, v, box, 8.0))
+        tasks.append((n, box, 1000 * seed + c, f, max(8, 625 // scale ** 3), tuple(contractions)))
+    if workers > 1 and n_cubes > 1:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+
+        with cf.ProcessPoolExecutor(min(workers, n_cubes), mp_context=mp.get_context("spawn")) as ex:
+            cubes = list(ex.map(_batch_cube, *zip(*tasks)))
+    else:
+        cubes = [_batch_cube(*t) for t in tasks]
+    items = [it for cube in cubes for it in cube]
     ncs = tuple(max(4, nc // scale) for nc in (32, 64, 128))
     return items, ncs
 

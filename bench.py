@@ -164,6 +164,84 @@ def cpu_reference_run(nthreads: int, cube, ncs):
     return time.perf_counter() - t0
 
 
+def knn_cube_counts(x, h, sample=200000, seed=5):
+    """Mean over a seeded sample of particles of C_i, the number of particles in
+    the cube of half-width h_i about particle i (itself included): the
+    candidates any exact 33-neighbour search must examine.  Returns (mean,
+    sample size)."""
+    from scipy.spatial import cKDTree
+
+    x = np.asarray(x, np.float64)
+    s = np.random.default_rng(seed).choice(len(x), min(sample, len(x)), replace=False)
+    cnt = cKDTree(x).query_ball_point(x[s], r=np.asarray(h, np.float64)[s], p=np.inf,
+                                      return_length=True, workers=os.cpu_count() or 1)
+    return float(np.mean(cnt)), int(len(s))
+
+
+def knn_sets(pos, qs, cand):
+    """The 33 nearest of each query qs among its candidates cand (n_q, m): keys
+    (d2, index) with d2 the reference's float32 expression, as sorted index sets."""
+    p = np.asarray(pos, np.float32)
+    d = p[cand] - p[qs][:, None, :]
+    d2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+    order = np.lexsort((cand, d2), axis=-1)
+    return np.sort(np.take_along_axis(cand, order[:, :33], axis=1), axis=1)
+
+
+def mesh_errors64(mesh, m64, nc):
+    """Largest relative errors of n and c (cells above 1e-3 of the mean n) and
+    of v against |v| + n on the same cells, against an FP64 mesh."""
+    nm = nc ** 3
+    n64, c64, v64 = m64[:nm], m64[2 * nm:3 * nm], m64[3 * nm:]
+    sel = n64 > 1e-3 * n64.mean()
+    out = {}
+    for name, a, ref in (("n", 0, n64), ("c", 2 * nm, c64)):
+        got = mesh[a:a + nm].astype(np.float64)
+        out[name] = float(np.max(np.abs(got[sel] - ref[sel]) / ref[sel]))
+    sv = np.repeat(sel, 3)
+    scale = (np.abs(v64) + np.repeat(n64, 3))[sv]
+    out["v"] = float(np.max(np.abs(mesh[3 * nm:].astype(np.float64)[sv] - v64[sv]) / scale))
+    return out
+
+
+def mixed_accuracy(cube, ncs, x_mixed, rk_plain, rk_mixed, dens_mixed, meshes_plain,
+                   meshes_mixed, nthreads, sample=20000):
+    """Accuracy of the mixed-precision form: neighbour-set agreement with the
+    FP32 form on a seeded sample of queries (the 33 nearest among the 48
+    nearest candidates of the original positions, each set by its own float32
+    distances), the relative change of h, and dens and the per-cell fields of
+    both forms against the FP64 oracle on the original positions (exact top-33,
+    FP64 dens over those lists, FP64 deposit with the oracle's rk and dens)."""
+    from scipy.spatial import cKDTree
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    x = np.asarray(cube.x, np.float32)
+    rng = np.random.default_rng(11)
+    qs = rng.choice(cube.n, min(sample, cube.n), replace=False)
+    _, cand = cKDTree(x.astype(np.float64)).query(x[qs].astype(np.float64), k=48, workers=nthreads)
+    same = np.all(knn_sets(x, qs, cand) == knn_sets(x_mixed, qs, cand), axis=1)
+    rel = np.abs(rk_mixed.astype(np.float64) - rk_plain) / rk_plain
+    O = pyoracle.Oracle()
+    te, _, nbr = O.knn_exact(x, cube.left, cube.right, nthreads)
+    rk_e, _, d64 = O.dens_from_lists(x, nbr, te)
+    del nbr
+    out = {"neighbour_sets_identical": {"fraction": float(same.mean()), "queries": int(len(qs))},
+           "h_rel_change_vs_fp32_positions": {"max": float(rel.max()),
+                                              "median": float(np.median(rel))},
+           "dens_rel_err_vs_fp64_oracle": float(np.max(np.abs(dens_mixed - d64) / d64)),
+           "mesh_rel_err_vs_fp64_oracle": {}}
+    ig = np.zeros(cube.n, np.int32)
+    for k, nc in enumerate(ncs):
+        _, m64, _ = O.assign_on_mesh(x, cube.v, d64.astype(np.float32), rk_e, ig, cube.boxsize, nc,
+                                     -1, nthreads=nthreads)
+        out["mesh_rel_err_vs_fp64_oracle"][str(nc)] = {
+            "mixed": mesh_errors64(meshes_mixed[k], m64, nc),
+            "plain": mesh_errors64(meshes_plain[k], m64, nc)}
+    return out
+
+
 def workload_config(wl_desc: str, cube) -> dict:
     """The `config` object of both arms' lines for one workload."""
     return {"workload": wl_desc + ", plain FP32 form", "n_with_shell": int(cube.n),
@@ -330,16 +408,19 @@ def run_ours(args):
         rk_d = torch.empty(n, dtype=torch.float32, device="cuda")
         ctx.store_fields_device(rk_ptr=rk_d.data_ptr())
         rk_host = rk_d.cpu().numpy()
+    # the plain form's meshes of the last run, for the mixed form's accuracy report
+    meshes_plain = [ctx.copy_mesh(k, 6 * nc ** 3) for k, nc in enumerate(ncs)]
 
     # roofline of the dominant kernel (measured live above)
     fp32 = ctx.measure_fp32_peak()
     pk, pk_kind = peaks()
     cells, tile_pairs = deposit_cells(cube.x, rk_host, cube.boxsize, ncs)
     dep_stats = ctx.deposit_stats()
+    c_mean, c_sample = knn_cube_counts(cube.x, rk_host)
     alg = {  # algorithmic FP32 flops per step, per phase
-        "knn_t33": 8.0 * 33 * 6 / np.pi * n,  # 8 flops per distance, ~63 candidates per query
-        "dens": 14.0 * 32 * n,                 # 14 flops per tent weight, 32 receivers per query
-        "deposit": 12.0 * cells,               # 12 flops per particle-cell pair
+        "knn_t33": 8.0 * c_mean * n,  # 8 flops per distance, C_i candidates per query
+        "dens": 14.0 * 32 * n,        # 14 flops per tent weight, 32 receivers per query
+        "deposit": 12.0 * cells,      # 12 flops per particle-cell pair
     }
     per_step = {k: v / args.steps for k, v in phases.items()}
     dom = max(("knn_t33", "deposit", "dens"), key=lambda k: per_step.get(k, 0.0))
@@ -354,13 +435,16 @@ def run_ours(args):
             traffic = rec["bytes_per_particle"] * n
             # what bounds the kernel instead of FMA throughput: ALU pipe and issue slots
             pipes = {k: rec[k] for k in ("alu_pipe_pct_of_peak", "fma_pipe_pct_of_peak",
-                                         "issue_active_pct", "kernel", "capture") if k in rec}
+                                         "tensor_pipe_pct_of_peak", "issue_active_pct", "kernel",
+                                         "capture") if k in rec}
     hbm_alg = n * (12 + 8 + 36) + sum(24 * nc ** 3 for nc in ncs)
     roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": fp32, "unit": "TFLOP/s",
             "frac": achieved / fp32, "traffic": traffic, "pipe_utilisation_ncu": pipes,
             "peak_source": "measured FMA-chain kernel on this GPU (no FP32 figure in the peaks file)",
             "phase_ms_per_step": per_step,
             "alg_flops_per_step": alg,
+            "knn_candidates_per_query": {"mean": c_mean, "sample": c_sample,
+                                         "definition": "C_i = #{j : |x_j - x_i|_inf <= h_i}"},
             "step_alg_hbm_bytes": hbm_alg,
             "deposit_work": dict(dep_stats, exact_particle_tile_pairs=tile_pairs,
                                  particle_cell_pairs=cells),
@@ -400,14 +484,23 @@ def run_ours(args):
 
         ms_m, phases_m, launches_m, _, _ = timed(step_mixed, False)
         rkm_d = torch.empty(n, dtype=torch.float32, device="cuda")
-        ctx.store_fields_device(rk_ptr=rkm_d.data_ptr())
-        rel = np.abs(rkm_d.cpu().numpy().astype(np.float64) - rk_host) / rk_host
+        dm_d = torch.empty(n, dtype=torch.float32, device="cuda")
+        ctx.store_fields_device(rk_ptr=rkm_d.data_ptr(), dens_ptr=dm_d.data_ptr())
+        rk_m = rkm_d.cpu().numpy()
+        rel = np.abs(rk_m.astype(np.float64) - rk_host) / rk_host
         mixed = {"value": replica_value(n_local, world, ms_m * 1e-3), "unit": "particles/s",
                  "ms_per_step": ms_m, "vs_plain": ms_step / ms_m, "gpu_launches": launches_m,
                  "phase_ms_per_step": {k: v / args.steps for k, v in phases_m.items()},
                  "input": "int32 cell index + 3 x uint16 offsets (4-unit cells) + float32 v",
                  "h_rel_err_vs_fp32_positions": {"max": float(rel.max()),
                                                  "median": float(np.median(rel))}}
+        if rank == 0 and world == 1 and not args.no_accuracy:
+            from asmooth_gb300.quantised import dequantise
+
+            meshes_m = [ctx.copy_mesh(k, 6 * nc ** 3) for k, nc in enumerate(ncs)]
+            mixed["accuracy"] = mixed_accuracy(
+                cube, ncs, dequantise(cell, off, grid, cube.left, 4.0), rk_host, rk_m,
+                dm_d.cpu().numpy(), meshes_plain, meshes_m, os.cpu_count() or 1)
         if not args.no_e2e:
             # inputs and outputs carved from one huge-page block
             parts = [((n,), np.int32), ((n, 3), np.uint16), ((n, 3), np.float32),
@@ -446,10 +539,12 @@ def run_ours(args):
 
     # batched form: the 27-cube x 3-redshift workload through one CUDA graph
     batch = None
-    if args.batch:
-        items, bncs = syn.make_batch(scale=args.batch_scale)
+    if not args.no_batch:
+        items, bncs = syn.make_batch(scale=args.batch_scale, workers=os.cpu_count() or 1)
         with api.Batch(ctx, items, bncs) as bt:
-            tuned = bt.tune() if args.tune else None
+            if not args.no_tune:
+                bt.tune()
+            tuned = bt.config()
             bt.set_streams(args.batch_streams)
             bt.run()  # plan, capture, first replay
             gms = []
@@ -464,7 +559,7 @@ def run_ours(args):
                  "particles_with_shell": int(sum(c.n for c in items)),
                  "graph_ms": g, "value": replica_value(st["particles_local"], world, g * 1e-3),
                  "unit": "particles/s", "kernels_per_graph": st["kernels"],
-                 "tuned_leaf_seg": tuned, "streams": args.batch_streams,
+                 "config": tuned, "tuned": not args.no_tune, "streams": args.batch_streams,
                  "workload": "27 cubes of side 256 (128^3 +- clustering-dependent count, halo "
                              "fraction U[0.2,0.8]) x 3 redshifts (halos contracted 1, 0.7, 0.5)"
                              + (f", scale 1/{args.batch_scale}" if args.batch_scale > 1 else "")}
@@ -519,16 +614,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the mixed form's accuracy report against the FP64 oracle")
     ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS),
                     help="cfg2_s2: the cfg2 model at 1/8 volume, for profiling captures; "
                          "cfg5: the 512^3 cube")
     ap.add_argument("--fof", action="store_true",
                     help="also time GPU FOF (linking length 0.4) on the loaded cube")
-    ap.add_argument("--batch", action="store_true",
-                    help="also time the batched form (27 cubes x 3 redshifts, one CUDA graph)")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched form (27 cubes x 3 redshifts, one CUDA graph)")
     ap.add_argument("--batch-scale", type=int, default=1,
                     help="divide the batched cubes' side by this (quick runs)")
-    ap.add_argument("--tune", action="store_true", help="autotune the batched form first")
+    ap.add_argument("--no-tune", action="store_true", help="skip autotuning the batched form")
     ap.add_argument("--batch-streams", type=int, default=4,
                     help="concurrent streams inside the batched form's graph")
     args = ap.parse_args()

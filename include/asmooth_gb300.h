@@ -305,9 +305,15 @@ int asg_batch_set_item(asg_batch* batch, int item, const float* x, const float* 
  * stream i % streams, each stream with its own scratch (about 300 bytes per
  * particle of the largest item), forked and joined inside the one graph. */
 int asg_batch_set_streams(asg_batch* batch, int streams);
-/* Optional autotuner: times the largest item with tree bucket sizes 16, 24, 32
- * and deposit work items of 2048, 4096, 8192 pairs and keeps the fastest. */
+/* Optional autotuner: times the largest item with tree bucket sizes 16, 24, 32,
+ * deposit work items of 2048, 4096, 8192 pairs, 2 or 4 warps per block of the
+ * neighbour search and the deposit on the tensor cores or the CUDA cores, and
+ * keeps the fastest; *leaf and *seg receive the first two choices. */
 int asg_batch_tune(asg_batch* batch, int* leaf, int* seg);
+/* The batch's configuration (tuned or default): tree bucket size, deposit
+ * work-item length, neighbour-search warps per block, 1 when the deposit runs
+ * on the tensor cores.  Any pointer may be NULL. */
+int asg_batch_config(asg_batch* batch, int* leaf, int* seg, int* knn_warps, int* tensor_deposit);
 int asg_batch_run(asg_batch* batch);
 /* Device time of the last graph launch (ms), kernels per launch, and the
  * interior particles of all items (the numerator of the batched metric). */

@@ -28,21 +28,6 @@ def exact_t33(x: np.ndarray, q: int):
     return d2[k], int(k)
 
 
-def dens_brute(x: np.ndarray, rk: np.ndarray, t33: np.ndarray, idx33: np.ndarray, j: int) -> float:
-    """dens of receiver j by brute force: the reference's float32 ker(q, j) of
-    every query q whose 32-set ((d2, index) below its 33rd key) holds j,
-    summed in float64."""
-    d2 = d2_to_all(x, x[j])  # d2(q, j) for every q (the squares of exact negations agree)
-    member = (d2 < t33) | ((d2 == t33) & (j < idx33))
-    q = np.nonzero(member)[0]
-    hinv = (np.float32(1.0) / rk[q].astype(np.float32)).astype(np.float32)
-    dx = np.abs(x[q].astype(np.float32) - x[j].astype(np.float32)).astype(np.float32)
-    w = (hinv * hinv).astype(np.float32) * hinv
-    for a in range(3):
-        w = (w * (np.float32(1.0) - (dx[:, a] * hinv).astype(np.float32))).astype(np.float32)
-    return float(np.sum(w.astype(np.float64)))
-
-
 def rel_err_cells(got: np.ndarray, ref: np.ndarray, weight: np.ndarray, frac: float = 1e-3):
     """Max relative error over cells whose weight exceeds frac x mean weight."""
     sel = weight > frac * weight.mean()

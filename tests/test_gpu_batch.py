@@ -78,6 +78,8 @@ def test_batch_tune(batch_items):
     with api.Context(0) as ctx, api.Batch(ctx, items[:3], ncs) as b:
         leaf, seg = b.tune()
         assert leaf in (16, 24, 32) and seg in (2048, 4096, 8192)
+        cfg = b.config()
+        assert (cfg["leaf"], cfg["seg"]) == (leaf, seg) and cfg["knn_warps"] in (2, 4)
         b.run()
         for i, cube in enumerate(items[:3]):
             rk, dens, meshes, tot = b.get(i)
@@ -103,3 +105,31 @@ def close_fields(a, r, nc):
             assert np.max(np.abs(x[sel] - y[sel]) / np.abs(y[sel])) <= FIELD_TOL
     v, vr = a[3 * nm:], r[3 * nm:]
     assert np.all(np.abs(v - vr) <= FIELD_TOL * (np.abs(vr) + np.repeat(n, 3)) + 1e-30)
+
+
+def test_batch_item_vs_oracle(batch_items, oracle):
+    """One item of the batched form against the CPU oracle directly: rk bit for
+    bit with the exact top-33 definition, dens within 1e-5 of the FP64 sum over
+    the oracle's lists, every mesh within 1e-5 of the FP64 restatement (cells
+    above 1e-3 of the mean density) and the FP64 masses within 1e-10."""
+    import os
+
+    from helpers import field_errors
+
+    items, ncs = batch_items
+    k = 4  # the second cube at the second redshift (halos contracted by 0.7)
+    cube = items[k]
+    with api.Context(0) as ctx, api.Batch(ctx, items, ncs) as b:
+        b.set_streams(2)
+        b.run()
+        rk, dens, meshes, tot = b.get(k)
+    te, _, nbr = oracle.knn_exact(cube.x, cube.left, cube.right, os.cpu_count() or 1)
+    assert np.array_equal(bits(rk), bits(np.sqrt(te)))
+    _, _, d64 = oracle.dens_from_lists(cube.x, nbr, te)
+    assert np.max(np.abs(dens - d64) / d64) <= FIELD_TOL
+    ig = np.zeros(cube.n, np.int32)
+    for m, t, nc in zip(meshes, tot, ncs):
+        _, m64, t64 = oracle.assign_on_mesh(cube.x, cube.v, dens, rk, ig, cube.boxsize, nc, -1)
+        errs = field_errors(m, m64, nc, False)
+        assert max(errs.values()) <= FIELD_TOL, errs
+        assert abs(t[0] - t64[0]) <= 1e-10 * t64[0]
