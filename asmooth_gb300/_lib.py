@@ -80,7 +80,7 @@ SIGNATURES = {
     "asg_deposit_stats": (_i, [_vp, _vp, _vp, _vp]),
     "asg_neighbor_search_noalloc": (_i, [_vp, _i, _f, _f, _vp, _vp, _vp]),
 }
-NPHASES = 8
+NPHASES = 10
 
 _LIB = None
 

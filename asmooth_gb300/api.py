@@ -512,7 +512,8 @@ class Batch:
         v = [C.c_int(0) for _ in range(4)]
         self.ctx._ok(self.lib.asg_batch_config(self.h, *[C.byref(x) for x in v]))
         return {"leaf": v[0].value, "seg": v[1].value, "knn_warps": v[2].value,
-                "tensor_deposit": bool(v[3].value)}
+                "deposit_engine": {0: "cuda cores", 1: "tensor cores, 1 warp per item",
+                                   2: "tensor cores, 2 warps per item"}.get(v[3].value, v[3].value)}
 
     def run(self):
         self.ctx._ok(self.lib.asg_batch_run(self.h))

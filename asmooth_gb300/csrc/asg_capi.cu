@@ -7,6 +7,7 @@
 #include <sys/mman.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <atomic>
 #include <climits>
 #include <cmath>
@@ -60,7 +61,7 @@ struct asg_ctx {
     int leaf = 32;  // tree bucket size scanned whole by the traversals (fastest on GB300)
     int dep_seg = 4096;  // pairs per deposit work item
     int knn_warps = 2;   // warps per block of the neighbour search (2 or 4)
-    int dep_mma = deposit_default_mma();  // deposit on the tensor cores (1) or CUDA cores (0)
+    int dep_mma = deposit_default_mma();  // deposit engine: tensor cores (1, 2) or CUDA cores (0)
     int* perm = nullptr;       // sorted position -> input index
     uint64_t* keys = nullptr;  // sorted keys
 
@@ -629,8 +630,10 @@ int asg_load_particles(asg_ctx* ctx, const asg_particle* p, int np, float left, 
     ctx->n = np;
     ctx->left = left;
     ctx->right = right;
+    phase_begin(ctx, ASG_PH_UPLOAD);
     CK(cudaMemcpyAsync(ctx->aos.p, p, sizeof(asg_particle) * (size_t)np, cudaMemcpyHostToDevice,
                        ctx->s));
+    phase_end(ctx);
     phase_begin(ctx, ASG_PH_INDEX);
     launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
                       P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
@@ -1040,15 +1043,18 @@ int asg_run_remove_small_groups(asg_ctx* ctx, int ngrp, int* nhalo)
 
 // cap == 0: size the pair arrays from the pair count (one host synchronisation);
 // cap > 0: pair arrays of that capacity, no synchronisation (stream capture)
+// slot0: the meshes go to ctx->meshes[slot0 ..] and their totals to
+// totals[2 slot0 ..] (a call per mesh keeps the other meshes' buffers)
 static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,
-                         int periodic, const int* coords, int density_only, uint32_t cap = 0)
+                         int periodic, const int* coords, int density_only, uint32_t cap = 0,
+                         int slot0 = 0)
 {
     if (!ncs || n_nc <= 0 || n_nc > MAX_MESHES) return fail(ctx, ASG_ERR_ARG, "1..8 meshes");
     if (!(boxsize > 0.0f) || !std::isfinite(boxsize)) return fail(ctx, ASG_ERR_ARG, "boxsize");
     for (int k = 0; k < n_nc; ++k)
         if (ncs[k] <= 0 || ncs[k] > 1290) return fail(ctx, ASG_ERR_ARG, "nc out of range");
     ensure_rk_checked(ctx);
-    if ((int)ctx->meshes.size() < n_nc) ctx->meshes.resize((size_t)n_nc);
+    if ((int)ctx->meshes.size() < slot0 + n_nc) ctx->meshes.resize((size_t)(slot0 + n_nc));
     ctx->mesh_boxsize = boxsize;
     DepositParams p;
     std::memset(&p, 0, sizeof(p));
@@ -1062,7 +1068,7 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     for (int d = 0; d < 3; ++d) p.offset[d] = periodic && coords ? boxsize * (float)coords[d] : 0.0f;
     int tiles = 0;
     for (int k = 0; k < n_nc; ++k) {
-        MeshBuf& mb = ctx->meshes[(size_t)k];
+        MeshBuf& mb = ctx->meshes[(size_t)(slot0 + k)];
         const int nc = ncs[k];
         const size_t nm = (size_t)nc * nc * nc * (density_only ? 1 : 6);
         const int tpd = (nc + 7) / 8;
@@ -1080,7 +1086,7 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
         j.partial = P<double>(mb.partial);
         tiles += tpd * tpd * tpd;
     }
-    if (int r = grow(ctx, ctx->totals, 16 * (size_t)n_nc)) return r;
+    if (int r = grow(ctx, ctx->totals, 16 * (size_t)(slot0 + n_nc))) return r;
     // particle records and pair counts, then size the pair arrays
     const int n = ctx->n;
     const size_t T1 = (size_t)tiles + 1;
@@ -1122,10 +1128,45 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     launch_deposit_run(n, p, tiles, npairs, cap != 0, w, ctx->d_err, ctx->s);
     for (int k = 0; k < n_nc; ++k) {
         const int tpd = (ncs[k] + 7) / 8;
-        launch_reduce_partials(P<double>(ctx->meshes[(size_t)k].partial), tpd * tpd * tpd,
-                               P<double>(ctx->totals) + 2 * k, ctx->s);
+        launch_reduce_partials(P<double>(ctx->meshes[(size_t)(slot0 + k)].partial), tpd * tpd * tpd,
+                               P<double>(ctx->totals) + 2 * (slot0 + k), ctx->s);
     }
     phase_end(ctx);
+    return 0;
+}
+
+// times (with timing on) the end of an end-to-end call: from the end of the
+// compute on the main stream until the copies on the output stream are done
+static void output_tail(asg_ctx* ctx)
+{
+    if (!ctx->timing) return;
+    phase_begin(ctx, ASG_PH_OUTPUT);
+    cudaEvent_t e = next_event(ctx);
+    cudaEventRecord(e, ctx->s_out);
+    cudaStreamWaitEvent(ctx->s, e, 0);
+    phase_end(ctx);
+}
+
+// The deposit of an end-to-end call: one mesh after another, the largest
+// first, each copied to the host on the output stream while the next one is
+// deposited (a mesh's sums do not depend on the other meshes of the call).
+static int queue_deposit_out(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,
+                             float* const* meshes)
+{
+    if (!ncs || n_nc <= 0 || n_nc > MAX_MESHES) return fail(ctx, ASG_ERR_ARG, "1..8 meshes");
+    int order[MAX_MESHES];
+    for (int k = 0; k < n_nc; ++k) order[k] = k;
+    std::stable_sort(order, order + n_nc, [&](int a, int b) { return ncs[a] > ncs[b]; });
+    for (int i = 0; i < n_nc; ++i) {
+        const int k = order[i];
+        if (int r = queue_deposit(ctx, boxsize, ncs + k, 1, sign, 0, nullptr, 0, 0, k)) return r;
+        if (meshes && meshes[k]) {
+            CK(cudaEventRecord(ctx->fields_ready, ctx->s));
+            CK(cudaStreamWaitEvent(ctx->s_out, ctx->fields_ready, 0));
+            CK(cudaMemcpyAsync(meshes[k], ctx->meshes[(size_t)k].mesh.p,
+                               4 * ctx->meshes[(size_t)k].words, cudaMemcpyDeviceToHost, ctx->s_out));
+        }
+    }
     return 0;
 }
 
@@ -1250,8 +1291,10 @@ static int load_for_deposit(asg_ctx* ctx, const asg_particle* p, int np)
     ctx->n = np;
     ctx->left = -INFINITY;
     ctx->right = INFINITY;
+    phase_begin(ctx, ASG_PH_UPLOAD);
     CK(cudaMemcpyAsync(ctx->aos.p, p, sizeof(asg_particle) * (size_t)np, cudaMemcpyHostToDevice,
                        ctx->s));
+    phase_end(ctx);
     phase_begin(ctx, ASG_PH_INDEX);
     launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
                       P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
@@ -1433,8 +1476,8 @@ int asg_phase_ms(asg_ctx* ctx, double* ms)
 
 const char* asg_phase_name(int phase)
 {
-    static const char* names[ASG_NPHASES] = {"index", "knn_t33", "knn_ties", "check_rk",
-                                             "dens",  "deposit", "halos",    "fof"};
+    static const char* names[ASG_NPHASES] = {"index", "knn_t33", "knn_ties", "check_rk", "dens",
+                                             "deposit", "halos", "fof", "upload", "output"};
     return (phase >= 0 && phase < ASG_NPHASES) ? names[phase] : "?";
 }
 
@@ -1506,8 +1549,10 @@ int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, f
     ctx->n = np;
     ctx->left = left;
     ctx->right = right;
+    phase_begin(ctx, ASG_PH_UPLOAD);
     CK(cudaMemcpyAsync(ctx->aos.p, p, sizeof(asg_particle) * (size_t)np, cudaMemcpyHostToDevice,
                        ctx->s));
+    phase_end(ctx);
     phase_begin(ctx, ASG_PH_INDEX);
     launch_unpack_aos(ctx->aos.p, np, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
                       P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
@@ -1523,13 +1568,10 @@ int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, f
                     P<int>(ctx->igrp), np, ctx->aos.p, ctx->s_out);
     CK(cudaMemcpyAsync(p, ctx->aos.p, sizeof(asg_particle) * (size_t)np, cudaMemcpyDeviceToHost,
                        ctx->s_out));
-    const int rd = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0);
-    CK(cudaStreamSynchronize(ctx->s_out));  // the records are in p before any return
+    const int rd = queue_deposit_out(ctx, boxsize, ncs, n_nc, sign, meshes);
+    if (!rd) output_tail(ctx);
+    CK(cudaStreamSynchronize(ctx->s_out));  // the records and meshes are out before any return
     if (rd) return rd;
-    for (int k = 0; k < n_nc; ++k)
-        if (meshes && meshes[k])
-            CK(cudaMemcpyAsync(meshes[k], ctx->meshes[(size_t)k].mesh.p,
-                               4 * ctx->meshes[(size_t)k].words, cudaMemcpyDeviceToHost, ctx->s));
     if (totals)
         CK(cudaMemcpyAsync(totals, ctx->totals.p, 16 * (size_t)n_nc, cudaMemcpyDeviceToHost, ctx->s));
     if (int r = finish(ctx, "smooth")) return r;
@@ -1554,7 +1596,9 @@ int asg_smooth_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off, con
     const int* dc = nullptr;
     const uint16_t* doff = nullptr;
     const float* dv = nullptr;
+    phase_begin(ctx, ASG_PH_UPLOAD);
     if (int r = stage_quant(ctx, cell, off, v, np, &dc, &doff, &dv)) return r;
+    phase_end(ctx);
     load_quant_device(ctx, dc, doff, dv, np, left, right, cell_size, grid);
     run_knn(ctx);
     // rk and dens are final: back to input order and out while the deposit runs
@@ -1567,13 +1611,10 @@ int asg_smooth_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off, con
                           P<float>(ctx->uf), P<float>(ctx->minin), nullptr, ctx->s_out);
     if (rk) CK(cudaMemcpyAsync(rk, ctx->uf.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s_out));
     if (dens) CK(cudaMemcpyAsync(dens, ctx->minin.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s_out));
-    const int rd = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0);
-    CK(cudaStreamSynchronize(ctx->s_out));  // rk and dens are in place before any return
+    const int rd = queue_deposit_out(ctx, boxsize, ncs, n_nc, sign, meshes);
+    if (!rd) output_tail(ctx);
+    CK(cudaStreamSynchronize(ctx->s_out));  // rk, dens and the meshes are out before any return
     if (rd) return rd;
-    for (int k = 0; k < n_nc; ++k)
-        if (meshes && meshes[k])
-            CK(cudaMemcpyAsync(meshes[k], ctx->meshes[(size_t)k].mesh.p,
-                               4 * ctx->meshes[(size_t)k].words, cudaMemcpyDeviceToHost, ctx->s));
     if (totals)
         CK(cudaMemcpyAsync(totals, ctx->totals.p, 16 * (size_t)n_nc, cudaMemcpyDeviceToHost, ctx->s));
     return finish(ctx, "smooth_quantised");
@@ -1864,7 +1905,7 @@ int asg_batch_tune(asg_batch* b, int* leaf, int* seg)
         if (b->np[(size_t)i] > b->np[(size_t)item]) item = i;
     // tree bucket size x deposit work-item length x neighbour-search warps per
     // block x deposit engine (tensor cores or CUDA cores)
-    const int leaves[] = {16, 24, 32}, segs[] = {2048, 4096, 8192}, warps[] = {2, 4}, mmas[] = {1, 0};
+    const int leaves[] = {16, 24, 32}, segs[] = {2048, 4096, 8192}, warps[] = {2, 4}, mmas[] = {1, 2, 0};
     float best = INFINITY;
     int bl = ctx->leaf, bs = ctx->dep_seg, bw = ctx->knn_warps, bm = ctx->dep_mma;
     for (int l : leaves)
@@ -1901,14 +1942,14 @@ int asg_batch_tune(asg_batch* b, int* leaf, int* seg)
     return finish(ctx, "batch tune");
 }
 
-int asg_batch_config(asg_batch* b, int* leaf, int* seg, int* knn_warps, int* tensor_deposit)
+int asg_batch_config(asg_batch* b, int* leaf, int* seg, int* knn_warps, int* deposit_engine)
 {
     if (!b) return ASG_ERR_ARG;
     const asg_ctx* ctx = b->ctx;
     if (leaf) *leaf = ctx->leaf;
     if (seg) *seg = ctx->dep_seg;
     if (knn_warps) *knn_warps = ctx->knn_warps;
-    if (tensor_deposit) *tensor_deposit = ctx->dep_mma;
+    if (deposit_engine) *deposit_engine = ctx->dep_mma;
     return ASG_OK;
 }
 

@@ -106,6 +106,11 @@ __device__ __forceinline__ AxisRange axis_range(float exlo, float exhi, const Me
 constexpr int FLAG_HALO = 1;  // sign*igrp > 0: deposit into the halo channel
 constexpr int FLAG_SKIP = 2;  // periodic particle outside [0, L) or a halo in an n-only mesh
 
+// One 32-byte record per particle: (x', y', z', h') and (dens, vx, vy, vz),
+// with x' the deposit position (plus the rank offset when periodic) and h' = h,
+// -h when the particle deposits into the halo channel, 0 when it deposits
+// nothing.  The cell-range edges (x' -+ h)/L and 1/h are recomputed from it
+// where they are needed (load_dep_rec), with the same rounded operations.
 __global__ void k_dep_prep(const float4* __restrict__ pos, const float4* __restrict__ vel,
                            const int* __restrict__ igrp, const float* __restrict__ rk, int n,
                            DepositParams P, float4* __restrict__ rec, int* err)
@@ -117,23 +122,34 @@ __global__ void k_dep_prep(const float4* __restrict__ pos, const float4* __restr
     const float h = rk[i];
     if (!(h > 0.0f && h < INFINITY)) atomicOr(err, ERR_ZERO_RK);
     const float L = P.boxsize;
-    int flags = ((P.sign * igrp[i]) > 0) ? FLAG_HALO : 0;
-    if (P.density_only && (flags & FLAG_HALO)) flags |= FLAG_SKIP;
+    const bool halo = (P.sign * igrp[i]) > 0;
+    bool skip = P.density_only && halo;
     float x = p.x, y = p.y, z = p.z;
     if (P.periodic) {  // global_mesh.cpp:52-61: skip outside the cube, then add the offset
-        if (x < 0.0f || x >= L || y < 0.0f || y >= L || z < 0.0f || z >= L) flags |= FLAG_SKIP;
+        if (x < 0.0f || x >= L || y < 0.0f || y >= L || z < 0.0f || z >= L) skip = true;
         x = __fadd_rn(x, P.offset[0]);
         y = __fadd_rn(y, P.offset[1]);
         z = __fadd_rn(z, P.offset[2]);
     }
-    if (!(h > 0.0f && h < INFINITY)) flags |= FLAG_SKIP;
-    const float hinv = __fdiv_rn(1.0f, h);
-    rec[4 * (size_t)i] = make_float4(x, y, z, hinv);
-    rec[4 * (size_t)i + 1] = make_float4(__fdiv_rn(__fsub_rn(x, h), L), __fdiv_rn(__fsub_rn(y, h), L),
-                                         __fdiv_rn(__fsub_rn(z, h), L), v.w);
-    rec[4 * (size_t)i + 2] = make_float4(__fdiv_rn(__fadd_rn(x, h), L), __fdiv_rn(__fadd_rn(y, h), L),
-                                         __fdiv_rn(__fadd_rn(z, h), L), v.x);
-    rec[4 * (size_t)i + 3] = make_float4(v.y, v.z, __int_as_float(flags), 0.0f);
+    if (!(h > 0.0f && h < INFINITY)) skip = true;
+    rec[2 * (size_t)i] = make_float4(x, y, z, skip ? 0.0f : (halo ? -h : h));
+    rec[2 * (size_t)i + 1] = make_float4(v.w, v.x, v.y, v.z);
+}
+
+// particle i's record as the deposit kernels use it: A = (x', 1/h), B = ((x'-h)/L,
+// dens), Cc = ((x'+h)/L, vx), D = (vy, vz, flags)
+__device__ __forceinline__ void load_dep_rec(const float4* __restrict__ rec, int i, float L,
+                                             float4& A, float4& B, float4& Cc, float4& D)
+{
+    const float4 a = rec[2 * (size_t)i], b = rec[2 * (size_t)i + 1];
+    const float h = fabsf(a.w);
+    const int flags = (a.w < 0.0f ? FLAG_HALO : 0) | (h > 0.0f ? 0 : FLAG_SKIP);
+    A = make_float4(a.x, a.y, a.z, __fdiv_rn(1.0f, h));
+    B = make_float4(__fdiv_rn(__fsub_rn(a.x, h), L), __fdiv_rn(__fsub_rn(a.y, h), L),
+                    __fdiv_rn(__fsub_rn(a.z, h), L), b.x);
+    Cc = make_float4(__fdiv_rn(__fadd_rn(a.x, h), L), __fdiv_rn(__fadd_rn(a.y, h), L),
+                     __fdiv_rn(__fadd_rn(a.z, h), L), b.y);
+    D = make_float4(b.z, b.w, __int_as_float(flags), 0.0f);
 }
 
 // ---------------------------------------------------------------------------
@@ -156,9 +172,9 @@ __global__ void k_pairs(const float4* __restrict__ rec, int n, DepositParams P,
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float4 b = rec[4 * (size_t)i + 1];
-    const float4 c = rec[4 * (size_t)i + 2];
-    const int flags = __float_as_int(rec[4 * (size_t)i + 3].z);
+    float4 a, b, c, d;
+    load_dep_rec(rec, i, P.boxsize, a, b, c, d);
+    const int flags = __float_as_int(d.z);
     uint32_t cnt = 0;
     uint32_t o = EMIT ? offs[i] : 0u;
     const bool periodic = P.periodic != 0;
@@ -424,10 +440,8 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                     const int i = pvals[j];
                     const int combo = (int)(pkeys[j] & ((1u << IMG_BITS) - 1u));
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
-                    const float4 A = rec[4 * (size_t)i];
-                    const float4 B = rec[4 * (size_t)i + 1];
-                    const float4 Cc = rec[4 * (size_t)i + 2];
-                    const float4 D = rec[4 * (size_t)i + 3];
+                    float4 A, B, Cc, D;
+                    load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
                     const float xs[3] = {A.x, A.y, A.z};
                     const float lo[3] = {B.x, B.y, B.z};
                     const float hi[3] = {Cc.x, Cc.y, Cc.z};
@@ -695,10 +709,8 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                     const int i = pvals[j];
                     const int combo = (int)(pkeys[j] & ((1u << IMG_BITS) - 1u));
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
-                    const float4 A = rec[4 * (size_t)i];
-                    const float4 B = rec[4 * (size_t)i + 1];
-                    const float4 Cc = rec[4 * (size_t)i + 2];
-                    const float4 D = rec[4 * (size_t)i + 3];
+                    float4 A, B, Cc, D;
+                    load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
                     const float xs[3] = {A.x, A.y, A.z};
                     const float lo[3] = {B.x, B.y, B.z};
                     const float hi[3] = {Cc.x, Cc.y, Cc.z};
@@ -846,6 +858,262 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
     }
 }
 
+// The same GEMM with the two warps of a CTA sharing one item: both warps set up
+// a chunk of 64 pairs (one pair per thread) in the CTA's staging, then each
+// warp runs the K steps for its own half of the tile's y rows (two row blocks,
+// 12 fragments) and keeps the double-float sums of its own 8 cells per lane.
+// Per CTA 27 KB of shared memory and per thread about half the fragments, so
+// about twice as many warps stay resident as with one warp per item.
+constexpr int MMA2_CHUNK = 64;  // pairs set up per chunk (one per thread)
+
+template <int NCH>
+struct Mma2Cta {
+    float acc[2][NCH == 1 ? 2 : 9][8][32];  // [warp][word][2 (y - 4 warp) + dz][lane]
+    float w[MMA2_CHUNK][WROW];
+    float v[MMA2_CHUNK][NCH == 1 ? 1 : 8];
+    uint32_t info[MMA2_CHUNK];
+    double tot[2][2];   // per warp: n and halo mass of the item
+    int item, tile;
+};
+
+template <int NCH>
+__global__ void __launch_bounds__(64)
+k_deposit_mma2(const float4* __restrict__ rec, DepositParams P, int total_tiles,
+               const uint32_t* __restrict__ item_off, const uint32_t* __restrict__ tstart,
+               const uint32_t* __restrict__ tcount, const uint32_t* __restrict__ pkeys,
+               const int* __restrict__ pvals, float* __restrict__ partial,
+               double* __restrict__ item_tot, int* __restrict__ next_item)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NW = NCH == 1 ? 2 : 9;
+    const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    Mma2Cta<NCH>& S = *reinterpret_cast<Mma2Cta<NCH>*>(smem_raw);
+    float(*acc)[8][32] = S.acc[wp];
+    const bool periodic = P.periodic != 0;
+    const uint32_t total_items = item_off[total_tiles];
+
+    for (;;) {
+        if (tid == 0) {
+            const int it = atomicAdd(next_item, 1);
+            S.item = it;
+            S.tile = (uint32_t)it < total_items ? upper_index(item_off, total_tiles + 1, (uint32_t)it) : -1;
+        }
+        __syncthreads();
+        const int item = S.item, tile = S.tile;
+        if ((uint32_t)item >= total_items) break;
+        const TileGeo geo = tile_geo(P, tile);
+        const MeshJob& J = P.job[geo.job];
+        const int nc = geo.nc;
+        const int seg = item - (int)item_off[tile];
+        const int nseg = (int)(item_off[tile + 1] - item_off[tile]);
+        const int j0 = (int)tstart[tile] + seg * P.seg;
+        const int j1 = (int)tstart[tile] + min((int)tcount[tile], (seg + 1) * P.seg);
+
+#pragma unroll
+        for (int k = 0; k < NW; ++k)
+#pragma unroll
+            for (int r = 0; r < 8; ++r) acc[k][r][lane] = 0.f;
+        float C[2][NCH][4];
+#pragma unroll
+        for (int mb = 0; mb < 2; ++mb)
+#pragma unroll
+            for (int ch = 0; ch < NCH; ++ch)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) C[mb][ch][i] = 0.f;
+        float tn_hi = 0.f, tn_lo = 0.f, th_hi = 0.f, th_lo = 0.f;
+
+        for (int c0 = j0; c0 < j1; c0 += MMA2_CHUNK) {
+            // ---- setup: one pair per thread (as in k_deposit_mma) ----
+            {
+                const int j = c0 + tid;
+                float* wl = S.w[tid];
+                float vals[NCH == 1 ? 1 : 6];
+#pragma unroll
+                for (int k = 0; k < (NCH == 1 ? 1 : 6); ++k) vals[k] = 0.f;
+#pragma unroll
+                for (int k = 0; k < 3 * TS; ++k) wl[k] = 0.f;
+                uint32_t info = 0;
+                if (j < j1) {
+                    const int i = pvals[j];
+                    const int combo = (int)(pkeys[j] & ((1u << IMG_BITS) - 1u));
+                    const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
+                    float4 A, B, Cc, D;
+                    load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
+                    const float xs[3] = {A.x, A.y, A.z};
+                    const float lo[3] = {B.x, B.y, B.z};
+                    const float hi[3] = {Cc.x, Cc.y, Cc.z};
+                    const float hinv = A.w;
+                    float mh = 1.0f, ml = 0.0f;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const AxisRange ar = axis_range(lo[a], hi[a], J, nc, periodic);
+                        const int k = ar.k_lo + dk[a];
+                        const int sh = k * nc + geo.O[a];
+                        const int r0 = max(ar.left - sh, 0), r1 = min(ar.right - sh, geo.E[a]);
+                        float fi = (float)(r0 + sh);
+                        float e0 = __fmul_rn(__fmaf_rn(fi, J.dx, -xs[a]), hinv);
+                        float sh_ = 0.f, sl_ = 0.f;
+                        for (int c = r0; c < r1; ++c) {
+                            fi = __fadd_rn(fi, 1.0f);
+                            const float e1 = __fmul_rn(__fmaf_rn(fi, J.dx, -xs[a]), hinv);
+                            const float wv = tent_integral_rn(e0, e1);
+                            wl[a * TS + c] = wv;
+                            two_sum_acc(sh_, sl_, wv);
+                            e0 = e1;
+                        }
+                        if (a == 0) { mh = sh_; ml = sl_; }
+                        else df_mul_df(mh, ml, sh_, sl_);
+                        if (a == 1 && r1 > r0) info = ((1u << r1) - 1u) & ~((1u << r0) - 1u);
+                    }
+                    const bool halo = (__float_as_int(D.z) & FLAG_HALO) != 0;
+                    if (info) info |= halo ? INFO_HALO : INFO_MAIN;
+                    if (!halo) {
+                        vals[0] = 1.0f;
+                        if constexpr (NCH > 1) {
+                            vals[2] = B.w;
+                            vals[3] = Cc.w;
+                            vals[4] = D.x;
+                            vals[5] = D.y;
+                        }
+                        two_sum_acc(tn_hi, tn_lo, mh);
+                        tn_lo = __fadd_rn(tn_lo, ml);
+                    } else {
+                        if constexpr (NCH > 1) vals[1] = 1.0f;
+                        two_sum_acc(th_hi, th_lo, mh);
+                        th_lo = __fadd_rn(th_lo, ml);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < (NCH == 1 ? 1 : 6); ++k) S.v[tid][k] = vals[k];
+                S.info[tid] = info;
+            }
+            __syncthreads();
+            // ---- K steps over the chunk, this warp's row blocks 2 wp and 2 wp + 1 ----
+            const int cnt = min(MMA2_CHUNK, j1 - c0);
+            for (int s8 = 0; s8 < cnt; s8 += 8) {
+                const uint32_t kinfo = __reduce_or_sync(FULLM, S.info[s8 + (lane & 7)]);
+                const uint32_t rows = 0xfu << (4 * wp);  // the y rows of this warp
+                if (!(kinfo & rows)) continue;
+                const float* wa = S.w[s8 + t];
+                const float* wb = S.w[s8 + t + 4];
+                const float xa = wa[g], xb = wb[g];
+                const float za = wa[2 * TS + g], zb = wb[2 * TS + g];
+                uint32_t bh[NCH][2], bl[NCH][2];
+#pragma unroll
+                for (int ch = 0; ch < NCH; ++ch) {
+                    if (!(kinfo & (ch == 1 && NCH > 1 ? INFO_HALO : INFO_MAIN))) continue;
+                    tf32_split(__fmul_rn(za, S.v[s8 + t][ch]), bh[ch][0], bl[ch][0]);
+                    tf32_split(__fmul_rn(zb, S.v[s8 + t + 4][ch]), bh[ch][1], bl[ch][1]);
+                }
+#pragma unroll
+                for (int m = 0; m < 2; ++m) {
+                    const int mb = 2 * wp + m;
+                    if (!(kinfo & (3u << (2 * mb)))) continue;
+                    uint32_t ah[4], al[4];
+                    tf32_split(__fmul_rn(xa, wa[TS + 2 * mb]), ah[0], al[0]);
+                    tf32_split(__fmul_rn(xa, wa[TS + 2 * mb + 1]), ah[1], al[1]);
+                    tf32_split(__fmul_rn(xb, wb[TS + 2 * mb]), ah[2], al[2]);
+                    tf32_split(__fmul_rn(xb, wb[TS + 2 * mb + 1]), ah[3], al[3]);
+#pragma unroll
+                    for (int ch = 0; ch < NCH; ++ch) {
+                        if (!(kinfo & (ch == 1 && NCH > 1 ? INFO_HALO : INFO_MAIN))) continue;
+                        mma_tf32(C[m][ch], al, bh[ch][0], bh[ch][1]);
+                        mma_tf32(C[m][ch], ah, bl[ch][0], bl[ch][1]);
+                        mma_tf32(C[m][ch], ah, bh[ch][0], bh[ch][1]);
+                    }
+                }
+            }
+            // ---- flush the fragments into the lane's sums (every chunk of 64 pairs) ----
+#pragma unroll
+            for (int m = 0; m < 2; ++m)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int r = 2 * (2 * m + (i >> 1)) + (i & 1);  // 2 (y - 4 wp) + dz
+                    float hi = acc[0][r][lane], lo = acc[1][r][lane];
+                    two_sum_acc(hi, lo, C[m][0][i]);
+                    acc[0][r][lane] = hi;
+                    acc[1][r][lane] = lo;
+                    C[m][0][i] = 0.f;
+                    if constexpr (NCH > 1) {
+                        hi = acc[4][r][lane]; lo = acc[5][r][lane];
+                        two_sum_acc(hi, lo, C[m][1][i]);
+                        acc[4][r][lane] = hi; acc[5][r][lane] = lo;
+                        hi = acc[2][r][lane]; lo = acc[3][r][lane];
+                        two_sum_acc(hi, lo, C[m][2][i]);
+                        acc[2][r][lane] = hi; acc[3][r][lane] = lo;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d)
+                            acc[6 + d][r][lane] = __fadd_rn(acc[6 + d][r][lane], C[m][3 + d][i]);
+#pragma unroll
+                        for (int ch = 1; ch < NCH; ++ch) C[m][ch][i] = 0.f;
+                    }
+                }
+            __syncthreads();  // the next chunk's setup overwrites the staging
+        }
+
+        // ---- the item's FP64 mass (both warps' setup lanes), then the cells ----
+        double sn = (double)tn_hi + (double)tn_lo, shl = (double)th_hi + (double)th_lo;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sn += __shfl_down_sync(FULLM, sn, o);
+            shl += __shfl_down_sync(FULLM, shl, o);
+        }
+        if (lane == 0) {
+            S.tot[wp][0] = sn;
+            S.tot[wp][1] = shl;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            sn = S.tot[0][0] + S.tot[1][0];
+            shl = S.tot[0][1] + S.tot[1][1];
+            if (nseg > 1) {
+                item_tot[2 * item] = sn;
+                item_tot[2 * item + 1] = shl;
+            } else {
+                J.partial[2 * geo.local] = sn;
+                J.partial[2 * geo.local + 1] = shl;
+            }
+        }
+        if (nseg > 1) {
+            float* pt = partial + (size_t)item * TC * PW;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int y = 4 * wp + (r >> 1), z = 2 * t + (r & 1);
+                const int e = (z * TS + y) * TS + g;
+                pt[e] = acc[0][r][lane];
+                pt[TC + e] = acc[1][r][lane];
+                if constexpr (NCH > 1) {
+                    pt[2 * TC + e] = acc[2][r][lane];
+                    pt[3 * TC + e] = acc[3][r][lane];
+                    pt[4 * TC + e] = acc[6][r][lane];
+                    pt[5 * TC + e] = acc[7][r][lane];
+                    pt[6 * TC + e] = acc[8][r][lane];
+                    pt[7 * TC + e] = acc[4][r][lane];
+                    pt[8 * TC + e] = acc[5][r][lane];
+                }
+            }
+        } else {
+            const size_t nmesh = (size_t)nc * nc * nc;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int y = 4 * wp + (r >> 1), z = 2 * t + (r & 1);
+                if (g >= geo.E[0] || y >= geo.E[1] || z >= geo.E[2]) continue;
+                const size_t idx = ((size_t)(geo.O[2] + z) * nc + (geo.O[1] + y)) * nc + (geo.O[0] + g);
+                J.mesh[idx] = __fadd_rn(acc[0][r][lane], acc[1][r][lane]);
+                if constexpr (NCH > 1) {
+                    J.mesh[nmesh + idx] = __fadd_rn(acc[4][r][lane], acc[5][r][lane]);
+                    J.mesh[2 * nmesh + idx] = __fadd_rn(acc[2][r][lane], acc[3][r][lane]);
+                    J.mesh[3 * nmesh + 3 * idx] = acc[6][r][lane];
+                    J.mesh[3 * nmesh + 3 * idx + 1] = acc[7][r][lane];
+                    J.mesh[3 * nmesh + 3 * idx + 2] = acc[8][r][lane];
+                }
+            }
+        }
+        __syncthreads();  // the next item's fetch overwrites S.item, S.tot
+    }
+}
+
 // ---------------------------------------------------------------------------
 // (5) merge the partial tiles of multi-segment tiles, in segment order
 // ---------------------------------------------------------------------------
@@ -912,7 +1180,7 @@ k_merge_tiles(DepositParams P, int total_tiles, const uint32_t* __restrict__ ite
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-size_t deposit_prep_bytes(int n) { return 64 * (size_t)n; }
+size_t deposit_prep_bytes(int n) { return 32 * (size_t)n; }
 
 size_t deposit_tile_bytes(int total_tiles)
 {
@@ -928,13 +1196,16 @@ static int key_bits(int total_tiles)
     return b + IMG_BITS;
 }
 
-// the default deposit engine: the tensor cores, or the CUDA cores with
-// ASG_DEPOSIT=simt (a comparison knob; a context's tuner may choose either)
+// the default deposit engine: 2 the tensor cores with the two warps of a CTA
+// per item, 1 with one warp per item, 0 the CUDA cores; ASG_DEPOSIT=mma2, mma
+// or simt selects one (a comparison knob; a context's tuner may choose)
 int deposit_default_mma()
 {
     static const int m = [] {
         const char* e = std::getenv("ASG_DEPOSIT");
-        return (e && std::strcmp(e, "simt") == 0) ? 0 : 1;
+        if (e && std::strcmp(e, "simt") == 0) return 0;
+        if (e && std::strcmp(e, "mma") == 0) return 1;
+        return 2;  // 15.3 against 15.6 ms (one warp per item) on the 256^3 step
     }();
     return m;
 }
@@ -1005,7 +1276,17 @@ void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     double* item_tot = nullptr;
-    if (p.mma) {
+    if (p.mma == 2) {
+        item_tot = deposit_item_totals(w.partial, deposit_max_items(T, npairs, p.seg));
+        if (p.density_only)
+            launch_persistent(k_deposit_mma2<1>, dev, sms, 64, sizeof(Mma2Cta<1>), s, w.rec, p, T,
+                              w.item_off, w.tstart, w.tcount, keys, vals, w.partial, item_tot,
+                              w.next_item);
+        else
+            launch_persistent(k_deposit_mma2<6>, dev, sms, 64, sizeof(Mma2Cta<6>), s, w.rec, p, T,
+                              w.item_off, w.tstart, w.tcount, keys, vals, w.partial, item_tot,
+                              w.next_item);
+    } else if (p.mma) {
         item_tot = deposit_item_totals(w.partial, deposit_max_items(T, npairs, p.seg));
         if (p.density_only)
             launch_persistent(k_deposit_mma<1>, dev, sms, 32 * MMA_WARPS,

@@ -8,6 +8,7 @@
 //
 // Determinism: the sort is stable and starts from input order, so equal keys
 // stay in input-index order; the tree is a pure function of the sorted keys.
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 
@@ -312,6 +313,22 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_count(const K* __restrict__ k
     counts[(size_t)threadIdx.x * ntiles + blockIdx.x] = hist[threadIdx.x];
 }
 
+// Stable scatter of one 8-bit digit.  A block takes a tile of RS_TILE elements;
+// warp w ranks its own contiguous RS_ROUNDS x 32 elements with per-warp digit
+// counters (no block barrier while ranking), one block-level scan turns the
+// counters into positions of the tile in digit order, the tile is placed in
+// shared memory in that order, and written out so that consecutive threads
+// store consecutive addresses within each digit's run.  Order is kept: within
+// a digit, elements stay in (warp, round, lane) = input order.
+template <class K>
+struct RsScatterSmem {
+    K key[RS_TILE];
+    int val[RS_TILE];
+    uint32_t wcnt[RS_THREADS / 32][256];  // per-warp digit counts, then offsets
+    uint32_t lstart[256];                 // first slot of each digit in the tile
+    uint32_t gstart[256];                 // the digit's first output position for this tile
+};
+
 template <class K>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const K* __restrict__ kin,
                                                            const int* __restrict__ vin,
@@ -321,42 +338,79 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const K* __restrict__
                                                            const uint32_t* __restrict__ offs,
                                                            int ntiles)
 {
-    __shared__ uint32_t run[256];
-    __shared__ uint32_t wcnt[RS_THREADS / 32][256];
-    run[threadIdx.x] = offs[(size_t)threadIdx.x * ntiles + blockIdx.x];
-    const int warp = threadIdx.x >> 5;
-    const unsigned lt = lanemask_lt();
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    RsScatterSmem<K>& S = *reinterpret_cast<RsScatterSmem<K>*>(rs_smem);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const unsigned lane = tid & 31, lt = lanemask_lt();
     const int base = blockIdx.x * RS_TILE;
-    for (int r = 0; r < RS_ROUNDS; ++r) {
-        const int i = base + r * RS_THREADS + threadIdx.x;
-        const bool valid = i < n;
-        const K k = valid ? kin[i] : (K)0;
-        const int v = valid ? vin[i] : 0;
-        const unsigned d = valid ? (unsigned)((k >> shift) & 255u) : 256u;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const unsigned rank = __popc(peers & lt);
-        for (int j = threadIdx.x; j < (RS_THREADS / 32) * 256; j += RS_THREADS)
-            (&wcnt[0][0])[j] = 0u;
-        __syncthreads();
-        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
-        __syncthreads();
-        {
-            uint32_t p = run[threadIdx.x];
 #pragma unroll
-            for (int w = 0; w < RS_THREADS / 32; ++w) {
-                const uint32_t c = wcnt[w][threadIdx.x];
-                wcnt[w][threadIdx.x] = p;
-                p += c;
-            }
-            run[threadIdx.x] = p;
+    for (int w = 0; w < RS_THREADS / 32; ++w) S.wcnt[w][tid] = 0u;
+    S.gstart[tid] = offs[(size_t)tid * ntiles + blockIdx.x];
+    __syncthreads();
+    // ---- rank: this warp's elements base + warp*32*ROUNDS + r*32 + lane ----
+    K k[RS_ROUNDS];
+    int v[RS_ROUNDS];
+    uint32_t pos[RS_ROUNDS];  // position among this warp's elements of the same digit
+    const int wbase = base + warp * 32 * RS_ROUNDS;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const int i = wbase + r * 32 + (int)lane;
+        const bool valid = i < n;
+        k[r] = valid ? kin[i] : (K)0;
+        v[r] = valid ? vin[i] : 0;
+        const unsigned d = valid ? (unsigned)((k[r] >> shift) & 255u) : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t before = valid ? S.wcnt[warp][d] : 0u;
+        pos[r] = before + __popc(peers & lt);
+        __syncwarp();
+        if (valid && (peers & lt) == 0u) S.wcnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // ---- per digit (thread = digit): offsets of the warps, then the tile's scan ----
+    {
+        uint32_t sum = 0;
+#pragma unroll
+        for (int w = 0; w < RS_THREADS / 32; ++w) {
+            const uint32_t c = S.wcnt[w][tid];
+            S.wcnt[w][tid] = sum;
+            sum += c;
         }
-        __syncthreads();
-        if (valid) {
-            const uint32_t dst = wcnt[warp][d] + rank;
-            kout[dst] = k;
-            vout[dst] = v;
+        // exclusive scan of the 256 digit totals (one per thread)
+        uint32_t inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if ((int)lane >= o) inc += y;
         }
+        __shared__ uint32_t wsum[RS_THREADS / 32];
+        if (lane == 31) wsum[warp] = inc;
         __syncthreads();
+        uint32_t woff = 0;
+        for (int w = 0; w < warp; ++w) woff += wsum[w];
+        S.lstart[tid] = woff + inc - sum;
+    }
+    __syncthreads();
+    // ---- place the tile in digit order ----
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const int i = wbase + r * 32 + (int)lane;
+        if (i < n) {
+            const unsigned d = (unsigned)((k[r] >> shift) & 255u);
+            const uint32_t slot = S.lstart[d] + S.wcnt[warp][d] + pos[r];
+            S.key[slot] = k[r];
+            S.val[slot] = v[r];
+        }
+    }
+    __syncthreads();
+    // ---- write out: slot j of digit d goes to gstart[d] + (j - lstart[d]) ----
+    const int cnt = min(RS_TILE, n - base);
+    for (int j = tid; j < cnt; j += RS_THREADS) {
+        const K kk = S.key[j];
+        const unsigned d = (unsigned)((kk >> shift) & 255u);
+        const uint32_t dst = S.gstart[d] + ((uint32_t)j - S.lstart[d]);
+        kout[dst] = kk;
+        vout[dst] = S.val[j];
     }
 }
 
@@ -373,6 +427,14 @@ static int radix_sort_t(K* keys0, int* vals0, K* keys1, int* vals1, int n, int b
 {
     if (n <= 1) return 0;
     const int ntiles = (n + RS_TILE - 1) / RS_TILE;
+    static std::atomic<unsigned long long> attr_set{0};  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!(attr_set.load() & (1ull << (dev & 63)))) {
+        cudaFuncSetAttribute(k_rs_scatter<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(RsScatterSmem<K>));
+        attr_set.fetch_or(1ull << (dev & 63));
+    }
     uint32_t* counts = (uint32_t*)temp;
     void* stemp = (void*)(counts + (size_t)256 * ntiles);
     K* kb[2] = {keys0, keys1};
@@ -381,8 +443,8 @@ static int radix_sort_t(K* keys0, int* vals0, K* keys1, int* vals1, int n, int b
     for (int shift = 0; shift < bits; shift += 8) {
         k_rs_count<K><<<ntiles, RS_THREADS, 0, s>>>(kb[cur], n, shift, counts, ntiles);
         exclusive_scan_u32(counts, (size_t)256 * ntiles, stemp, s);
-        k_rs_scatter<K><<<ntiles, RS_THREADS, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1],
-                                                      n, shift, counts, ntiles);
+        k_rs_scatter<K><<<ntiles, RS_THREADS, sizeof(RsScatterSmem<K>), s>>>(
+            kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n, shift, counts, ntiles);
         count_launches(2);
         cur ^= 1;
     }

@@ -121,11 +121,12 @@ struct DepositParams {
     float offset[3];  // periodic: rank cube offset
     int density_only;
     int seg;          // pairs per work item of the persistent deposit (tuning, > 0)
-    int mma;          // 1: the tensor-core deposit, 0: the CUDA-core one (tuning)
+    int mma;          // the deposit engine: 1 or 2 tensor cores (one or two warps per
+                      // item), 0 the CUDA cores (tuning)
 };
 // scratch of one deposit: particle records, (tile, image) pairs, work items
 struct DepositScratch {
-    float4* rec;          // [4n] x', hinv | (x-h)/L, dens | (x+h)/L, vx | vy, vz, flags
+    float4* rec;          // [2n] x', y', z', h (-h: halo channel, 0: skipped) | dens, v
     uint32_t* pcount;     // [n+1] pairs per particle, then their exclusive scan
     void* scan_tmp_n;     // scan scratch for n+1 entries
     uint32_t* keys0;      // [npairs] tile << 5 | image, ping-pong with keys1

@@ -453,7 +453,7 @@ def run_ours(args):
 
     # friends-of-friends beside the path (linking length 0.2 x mean separation 2)
     fof = None
-    if args.fof:
+    if not args.no_fof:
         ctx.load_particles_device(x_d.data_ptr(), n, cube.left, cube.right, v_ptr=v_d.data_ptr())
         ng = ctx.run_fof(0.4)
         ms_f = []
@@ -535,7 +535,9 @@ def run_ours(args):
             mixed["e2e"] = {"value": replica_value(n_local, world, tt), "unit": "particles/s",
                             "h2d_bytes_per_step": 22 * n,
                             "d2h_bytes_per_step": 8 * n + sum(4 * 6 * nc ** 3 for nc in ncs)
-                            + 16 * len(ncs)}
+                            + 16 * len(ncs),
+                            "call_ms": {"min": 1e3 * min(times), "median": 1e3 * statistics.median(times),
+                                        "max": 1e3 * max(times)}}
 
     # batched form: the 27-cube x 3-redshift workload through one CUDA graph
     batch = None
@@ -619,8 +621,8 @@ def main():
     ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS),
                     help="cfg2_s2: the cfg2 model at 1/8 volume, for profiling captures; "
                          "cfg5: the 512^3 cube")
-    ap.add_argument("--fof", action="store_true",
-                    help="also time GPU FOF (linking length 0.4) on the loaded cube")
+    ap.add_argument("--no-fof", action="store_true",
+                    help="skip timing GPU FOF (linking length 0.4) on the loaded cube")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched form (27 cubes x 3 redshifts, one CUDA graph)")
     ap.add_argument("--batch-scale", type=int, default=1,

@@ -307,13 +307,14 @@ int asg_batch_set_item(asg_batch* batch, int item, const float* x, const float* 
 int asg_batch_set_streams(asg_batch* batch, int streams);
 /* Optional autotuner: times the largest item with tree bucket sizes 16, 24, 32,
  * deposit work items of 2048, 4096, 8192 pairs, 2 or 4 warps per block of the
- * neighbour search and the deposit on the tensor cores or the CUDA cores, and
- * keeps the fastest; *leaf and *seg receive the first two choices. */
+ * neighbour search and each deposit engine, and keeps the fastest; *leaf and
+ * *seg receive the first two choices. */
 int asg_batch_tune(asg_batch* batch, int* leaf, int* seg);
 /* The batch's configuration (tuned or default): tree bucket size, deposit
- * work-item length, neighbour-search warps per block, 1 when the deposit runs
- * on the tensor cores.  Any pointer may be NULL. */
-int asg_batch_config(asg_batch* batch, int* leaf, int* seg, int* knn_warps, int* tensor_deposit);
+ * work-item length, neighbour-search warps per block and the deposit engine
+ * (1 or 2: tensor cores with one or two warps per tile item; 0: CUDA cores).
+ * Any pointer may be NULL. */
+int asg_batch_config(asg_batch* batch, int* leaf, int* seg, int* knn_warps, int* deposit_engine);
 int asg_batch_run(asg_batch* batch);
 /* Device time of the last graph launch (ms), kernels per launch, and the
  * interior particles of all items (the numerator of the batched metric). */
@@ -333,9 +334,12 @@ long long asg_kernel_launches(asg_ctx* ctx);
 /* Phase timing with CUDA events on the context stream.  enable != 0 turns it on
  * and zeroes the accumulators; asg_phase_ms fills ms[0..ASG_NPHASES-1] with the
  * device time accumulated per phase since then. */
-#define ASG_NPHASES 8
+#define ASG_NPHASES 10
+/* UPLOAD: the host-to-device copy of an end-to-end call's inputs; OUTPUT: from
+ * the end of its last deposit until its copies to the host are done. */
 enum { ASG_PH_INDEX = 0, ASG_PH_KNN = 1, ASG_PH_TIES = 2, ASG_PH_CHECK = 3, ASG_PH_DENS = 4,
-       ASG_PH_DEPOSIT = 5, ASG_PH_HALOS = 6, ASG_PH_FOF = 7 };
+       ASG_PH_DEPOSIT = 5, ASG_PH_HALOS = 6, ASG_PH_FOF = 7, ASG_PH_UPLOAD = 8,
+       ASG_PH_OUTPUT = 9 };
 int asg_set_timing(asg_ctx* ctx, int enable);
 int asg_phase_ms(asg_ctx* ctx, double* ms);
 const char* asg_phase_name(int phase);
