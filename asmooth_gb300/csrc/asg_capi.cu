@@ -1043,18 +1043,15 @@ int asg_run_remove_small_groups(asg_ctx* ctx, int ngrp, int* nhalo)
 
 // cap == 0: size the pair arrays from the pair count (one host synchronisation);
 // cap > 0: pair arrays of that capacity, no synchronisation (stream capture)
-// slot0: the meshes go to ctx->meshes[slot0 ..] and their totals to
-// totals[2 slot0 ..] (a call per mesh keeps the other meshes' buffers)
 static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,
-                         int periodic, const int* coords, int density_only, uint32_t cap = 0,
-                         int slot0 = 0)
+                         int periodic, const int* coords, int density_only, uint32_t cap = 0)
 {
     if (!ncs || n_nc <= 0 || n_nc > MAX_MESHES) return fail(ctx, ASG_ERR_ARG, "1..8 meshes");
     if (!(boxsize > 0.0f) || !std::isfinite(boxsize)) return fail(ctx, ASG_ERR_ARG, "boxsize");
     for (int k = 0; k < n_nc; ++k)
         if (ncs[k] <= 0 || ncs[k] > 1290) return fail(ctx, ASG_ERR_ARG, "nc out of range");
     ensure_rk_checked(ctx);
-    if ((int)ctx->meshes.size() < slot0 + n_nc) ctx->meshes.resize((size_t)(slot0 + n_nc));
+    if ((int)ctx->meshes.size() < n_nc) ctx->meshes.resize((size_t)n_nc);
     ctx->mesh_boxsize = boxsize;
     DepositParams p;
     std::memset(&p, 0, sizeof(p));
@@ -1068,7 +1065,7 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     for (int d = 0; d < 3; ++d) p.offset[d] = periodic && coords ? boxsize * (float)coords[d] : 0.0f;
     int tiles = 0;
     for (int k = 0; k < n_nc; ++k) {
-        MeshBuf& mb = ctx->meshes[(size_t)(slot0 + k)];
+        MeshBuf& mb = ctx->meshes[(size_t)k];
         const int nc = ncs[k];
         const size_t nm = (size_t)nc * nc * nc * (density_only ? 1 : 6);
         const int tpd = (nc + 7) / 8;
@@ -1086,7 +1083,7 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
         j.partial = P<double>(mb.partial);
         tiles += tpd * tpd * tpd;
     }
-    if (int r = grow(ctx, ctx->totals, 16 * (size_t)(slot0 + n_nc))) return r;
+    if (int r = grow(ctx, ctx->totals, 16 * (size_t)n_nc)) return r;
     // particle records and pair counts, then size the pair arrays
     const int n = ctx->n;
     const size_t T1 = (size_t)tiles + 1;
@@ -1128,45 +1125,33 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     launch_deposit_run(n, p, tiles, npairs, cap != 0, w, ctx->d_err, ctx->s);
     for (int k = 0; k < n_nc; ++k) {
         const int tpd = (ncs[k] + 7) / 8;
-        launch_reduce_partials(P<double>(ctx->meshes[(size_t)(slot0 + k)].partial), tpd * tpd * tpd,
-                               P<double>(ctx->totals) + 2 * (slot0 + k), ctx->s);
+        launch_reduce_partials(P<double>(ctx->meshes[(size_t)k].partial), tpd * tpd * tpd,
+                               P<double>(ctx->totals) + 2 * k, ctx->s);
     }
     phase_end(ctx);
     return 0;
 }
 
-// times (with timing on) the end of an end-to-end call: from the end of the
-// compute on the main stream until the copies on the output stream are done
-static void output_tail(asg_ctx* ctx)
+// The meshes of an end-to-end call to the host, on the output stream after the
+// deposit (timed as the output phase: from the end of the deposit until the
+// copies are done).  Depositing the meshes one at a time to overlap their
+// copies with the next deposit was measured and dropped: the three deposits
+// cost 3.6 ms more than one on the 256^3 step, the copies about 2.
+static int queue_mesh_out(asg_ctx* ctx, int n_nc, float* const* meshes)
 {
-    if (!ctx->timing) return;
     phase_begin(ctx, ASG_PH_OUTPUT);
-    cudaEvent_t e = next_event(ctx);
-    cudaEventRecord(e, ctx->s_out);
-    cudaStreamWaitEvent(ctx->s, e, 0);
-    phase_end(ctx);
-}
-
-// The deposit of an end-to-end call: one mesh after another, the largest
-// first, each copied to the host on the output stream while the next one is
-// deposited (a mesh's sums do not depend on the other meshes of the call).
-static int queue_deposit_out(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, int sign,
-                             float* const* meshes)
-{
-    if (!ncs || n_nc <= 0 || n_nc > MAX_MESHES) return fail(ctx, ASG_ERR_ARG, "1..8 meshes");
-    int order[MAX_MESHES];
-    for (int k = 0; k < n_nc; ++k) order[k] = k;
-    std::stable_sort(order, order + n_nc, [&](int a, int b) { return ncs[a] > ncs[b]; });
-    for (int i = 0; i < n_nc; ++i) {
-        const int k = order[i];
-        if (int r = queue_deposit(ctx, boxsize, ncs + k, 1, sign, 0, nullptr, 0, 0, k)) return r;
-        if (meshes && meshes[k]) {
-            CK(cudaEventRecord(ctx->fields_ready, ctx->s));
-            CK(cudaStreamWaitEvent(ctx->s_out, ctx->fields_ready, 0));
+    CK(cudaEventRecord(ctx->fields_ready, ctx->s));
+    CK(cudaStreamWaitEvent(ctx->s_out, ctx->fields_ready, 0));
+    for (int k = 0; k < n_nc; ++k)
+        if (meshes && meshes[k])
             CK(cudaMemcpyAsync(meshes[k], ctx->meshes[(size_t)k].mesh.p,
                                4 * ctx->meshes[(size_t)k].words, cudaMemcpyDeviceToHost, ctx->s_out));
-        }
+    if (ctx->timing) {
+        cudaEvent_t e = next_event(ctx);
+        cudaEventRecord(e, ctx->s_out);
+        cudaStreamWaitEvent(ctx->s, e, 0);
     }
+    phase_end(ctx);
     return 0;
 }
 
@@ -1568,8 +1553,8 @@ int asg_smooth(asg_ctx* ctx, asg_particle* p, int np, float left, float right, f
                     P<int>(ctx->igrp), np, ctx->aos.p, ctx->s_out);
     CK(cudaMemcpyAsync(p, ctx->aos.p, sizeof(asg_particle) * (size_t)np, cudaMemcpyDeviceToHost,
                        ctx->s_out));
-    const int rd = queue_deposit_out(ctx, boxsize, ncs, n_nc, sign, meshes);
-    if (!rd) output_tail(ctx);
+    const int rd = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0);
+    if (!rd) queue_mesh_out(ctx, n_nc, meshes);
     CK(cudaStreamSynchronize(ctx->s_out));  // the records and meshes are out before any return
     if (rd) return rd;
     if (totals)
@@ -1611,8 +1596,8 @@ int asg_smooth_quantised(asg_ctx* ctx, const int* cell, const uint16_t* off, con
                           P<float>(ctx->uf), P<float>(ctx->minin), nullptr, ctx->s_out);
     if (rk) CK(cudaMemcpyAsync(rk, ctx->uf.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s_out));
     if (dens) CK(cudaMemcpyAsync(dens, ctx->minin.p, 4 * n, cudaMemcpyDeviceToHost, ctx->s_out));
-    const int rd = queue_deposit_out(ctx, boxsize, ncs, n_nc, sign, meshes);
-    if (!rd) output_tail(ctx);
+    const int rd = queue_deposit(ctx, boxsize, ncs, n_nc, sign, 0, nullptr, 0);
+    if (!rd) queue_mesh_out(ctx, n_nc, meshes);
     CK(cudaStreamSynchronize(ctx->s_out));  // rk, dens and the meshes are out before any return
     if (rd) return rd;
     if (totals)

@@ -287,8 +287,11 @@ void exclusive_scan_u32(uint32_t* data, size_t n, void* temp, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // stable LSD radix sort, 8-bit digits
 // ---------------------------------------------------------------------------
+#ifndef ASG_RS_ROUNDS
+#define ASG_RS_ROUNDS 8
+#endif
 constexpr int RS_THREADS = 256;
-constexpr int RS_ROUNDS = 16;
+constexpr int RS_ROUNDS = ASG_RS_ROUNDS;  // elements per thread of a tile
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 
 template <class K>

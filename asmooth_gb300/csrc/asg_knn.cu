@@ -23,6 +23,7 @@
 //               receiver and bucket): exact integer sums, so deterministic in
 //               any order.  It visits the buckets k_knn_t33 recorded.
 #include <climits>
+#include <type_traits>
 
 #include "asg_common.cuh"
 #include "asg_internal.h"
@@ -367,7 +368,9 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
 
     // the bucket [first, last] (box from its node record, or a single particle)
     // against the queries of mask M
-    auto scan = [&](int first, int last, unsigned M) {
+    // the index rule of the 33rd key only matters in a bundle with a tied query
+    const bool any_tie = __any_sync(FULL, valid && idx33[q] >= 0);
+    auto scan = [&](int first, int last, unsigned M, auto ties) {
         const int cnt = last - first + 1;
         const bool have = lane < cnt;
         const int j = first + (have ? lane : 0);
@@ -383,7 +386,8 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
             // norm2 (nbr_search.cpp:20-25) and ker (:27-37) of (q, j), query first
             const float dx = __fsub_rn(Q.x, c.x), dy = __fsub_rn(Q.y, c.y), dz = __fsub_rn(Q.z, c.z);
             const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            const bool member = d2 < Q.w || (d2 == Q.w && cj < __float_as_int(A.z));
+            bool member = d2 < Q.w;
+            if constexpr (decltype(ties)::value) member = member || (d2 == Q.w && cj < __float_as_int(A.z));
             float w = A.y;
             w = __fmul_rn(w, __fsub_rn(1.0f, __fmul_rn(fabsf(dx), A.x)));
             w = __fmul_rn(w, __fsub_rn(1.0f, __fmul_rn(fabsf(dy), A.x)));
@@ -430,7 +434,8 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
             if (!M) continue;
             int first, last;
             bucket_range(node, first, last);
-            scan(first, last, M);
+            if (any_tie) scan(first, last, M, std::true_type{});
+            else scan(first, last, M, std::false_type{});
         }
         return;
     }
@@ -461,7 +466,8 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
         if (!M) continue;
         int first, last;
         bucket_range(node, first, last);
-        scan(first, last, M);
+        if (any_tie) scan(first, last, M, std::true_type{});
+        else scan(first, last, M, std::false_type{});
     }
 }
 
