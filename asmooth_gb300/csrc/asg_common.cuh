@@ -39,6 +39,52 @@ __device__ __forceinline__ float norm2_rn(float ax, float ay, float az, float bx
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
+// Pairs of floats in one 64-bit register (first element in the low half),
+// operated on by the packed f32x2 instructions: one instruction does both IEEE
+// single operations, each element rounded to nearest exactly as __fadd_rn /
+// __fsub_rn do.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pack2(float lo, float hi)
+{
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float lo2(f32x2 v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float hi2(f32x2 v) { return __uint_as_float((unsigned)(v >> 32)); }
+__device__ __forceinline__ f32x2 add2_rn(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 sub2_rn(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+// fl(d * d) as one packed fma with a +0 addend.  A packed mul followed by a
+// packed add is fused into one fma by the code generator even with explicit
+// rounding (measured: a quarter of the sums of two squares differ from the
+// scalar __fmul_rn / __fadd_rn result), which the fma form does not allow.  A
+// square is never -0, so the +0 addend leaves every rounded product unchanged.
+__device__ __forceinline__ f32x2 sq2_rn(f32x2 d)
+{
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(r) : "l"(d), "l"(0ull));
+    return r;
+}
+
+// norm2_rn from the point (ax, ay, az), each coordinate given twice, to two
+// points (their x, y and z pairs): the same roundings in the same order
+__device__ __forceinline__ f32x2 norm2_rn_x2(f32x2 ax, f32x2 ay, f32x2 az, f32x2 bx, f32x2 by,
+                                             f32x2 bz)
+{
+    const f32x2 dx = sub2_rn(ax, bx), dy = sub2_rn(ay, by), dz = sub2_rn(az, bz);
+    return add2_rn(add2_rn(sq2_rn(dx), sq2_rn(dy)), sq2_rn(dz));
+}
+
 // ker (nbr_search.cpp:27-37): hinv*hinv*hinv*(1-|dx|*hinv)*(1-|dy|*hinv)*(1-|dz|*hinv)
 __device__ __forceinline__ float ker_rn(float ax, float ay, float az, float bx, float by, float bz, float hinv)
 {

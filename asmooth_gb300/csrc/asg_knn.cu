@@ -88,7 +88,7 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
           float* __restrict__ rk, int* __restrict__ idx33, int* __restrict__ blist, int* err)
 {
     __shared__ int stk[T33_WARPS][STACK_MAX];
-    __shared__ float4 cand[T33_WARPS][32];
+    __shared__ __align__(16) float cand[T33_WARPS][3][32];  // x, y, z of the bucket's particles
     __shared__ float queue[T33_WARPS][KNN_QUEUE][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = t.n;
@@ -157,16 +157,27 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
         }
         const int cnt = last - first + 1;
         // an odd bucket is padded with a NaN point, whose distance queues nowhere
-        if (lane < cnt) cand[warp][lane] = pos[first + lane];
-        else if (lane == cnt) cand[warp][lane] = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+        if (lane < cnt) {
+            const float4 p = pos[first + lane];
+            cand[warp][0][lane] = p.x;
+            cand[warp][1][lane] = p.y;
+            cand[warp][2][lane] = p.z;
+        } else if (lane == cnt) {
+            cand[warp][0][lane] = __int_as_float(0x7fc00000);
+            cand[warp][1][lane] = 0.0f;
+            cand[warp][2][lane] = 0.0f;
+        }
         __syncwarp();
-        // two candidates per step, then one check: every queue holds at most
-        // KNN_QUEUE - 2 values when a step begins (equal values queue too: the
-        // merge tracks ties)
+        // two candidates per step (their distances in packed f32x2 operations),
+        // then one check: every queue holds at most KNN_QUEUE - 2 values when a
+        // step begins (equal values queue too: the merge tracks ties)
+        const f32x2 qx = pack2(xq.x, xq.x), qy = pack2(xq.y, xq.y), qz = pack2(xq.z, xq.z);
+        const f32x2* cx = reinterpret_cast<const f32x2*>(cand[warp][0]);
+        const f32x2* cy = reinterpret_cast<const f32x2*>(cand[warp][1]);
+        const f32x2* cz = reinterpret_cast<const f32x2*>(cand[warp][2]);
         for (int j = 0; j < cnt; j += 2) {
-            const float4 c0 = cand[warp][j], c1 = cand[warp][j + 1];
-            const float d0 = norm2_rn(xq.x, xq.y, xq.z, c0.x, c0.y, c0.z);
-            const float d1 = norm2_rn(xq.x, xq.y, xq.z, c1.x, c1.y, c1.z);
+            const f32x2 d2 = norm2_rn_x2(qx, qy, qz, cx[j >> 1], cy[j >> 1], cz[j >> 1]);
+            const float d0 = lo2(d2), d1 = hi2(d2);
             const float top = a[K_NN - 1];
             if (d0 <= top) qb[32 * qn++] = d0;
             if (d1 <= top) qb[32 * qn++] = d1;
