@@ -999,12 +999,24 @@ k_deposit_mma2(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                 const float* wb = S.w[s8 + t + 4];
                 const float xa = wa[g], xb = wb[g];
                 const float za = wa[2 * TS + g], zb = wb[2 * TS + g];
+                // the channels fed by main particles (n, c, v) and by halo
+                // particles (halo) are tested once each, and within a group the
+                // three passes run pass by pass over its channels, so the
+                // independent accumulation chains interleave
+                const bool k_main = (kinfo & INFO_MAIN) != 0;
+                const bool k_halo = NCH > 1 && (kinfo & INFO_HALO) != 0;
                 uint32_t bh[NCH][2], bl[NCH][2];
+                if (k_main) {
 #pragma unroll
-                for (int ch = 0; ch < NCH; ++ch) {
-                    if (!(kinfo & (ch == 1 && NCH > 1 ? INFO_HALO : INFO_MAIN))) continue;
-                    tf32_split(__fmul_rn(za, S.v[s8 + t][ch]), bh[ch][0], bl[ch][0]);
-                    tf32_split(__fmul_rn(zb, S.v[s8 + t + 4][ch]), bh[ch][1], bl[ch][1]);
+                    for (int ch = 0; ch < NCH; ++ch) {
+                        if (NCH > 1 && ch == 1) continue;
+                        tf32_split(__fmul_rn(za, S.v[s8 + t][ch]), bh[ch][0], bl[ch][0]);
+                        tf32_split(__fmul_rn(zb, S.v[s8 + t + 4][ch]), bh[ch][1], bl[ch][1]);
+                    }
+                }
+                if (k_halo) {
+                    tf32_split(__fmul_rn(za, S.v[s8 + t][1]), bh[1][0], bl[1][0]);
+                    tf32_split(__fmul_rn(zb, S.v[s8 + t + 4][1]), bh[1][1], bl[1][1]);
                 }
 #pragma unroll
                 for (int m = 0; m < 2; ++m) {
@@ -1015,12 +1027,21 @@ k_deposit_mma2(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                     tf32_split(__fmul_rn(xa, wa[TS + 2 * mb + 1]), ah[1], al[1]);
                     tf32_split(__fmul_rn(xb, wb[TS + 2 * mb]), ah[2], al[2]);
                     tf32_split(__fmul_rn(xb, wb[TS + 2 * mb + 1]), ah[3], al[3]);
+                    if (k_main) {
 #pragma unroll
-                    for (int ch = 0; ch < NCH; ++ch) {
-                        if (!(kinfo & (ch == 1 && NCH > 1 ? INFO_HALO : INFO_MAIN))) continue;
-                        mma_tf32(C[m][ch], al, bh[ch][0], bh[ch][1]);
-                        mma_tf32(C[m][ch], ah, bl[ch][0], bl[ch][1]);
-                        mma_tf32(C[m][ch], ah, bh[ch][0], bh[ch][1]);
+                        for (int ch = 0; ch < NCH; ++ch)
+                            if (!(NCH > 1 && ch == 1)) mma_tf32(C[m][ch], al, bh[ch][0], bh[ch][1]);
+#pragma unroll
+                        for (int ch = 0; ch < NCH; ++ch)
+                            if (!(NCH > 1 && ch == 1)) mma_tf32(C[m][ch], ah, bl[ch][0], bl[ch][1]);
+#pragma unroll
+                        for (int ch = 0; ch < NCH; ++ch)
+                            if (!(NCH > 1 && ch == 1)) mma_tf32(C[m][ch], ah, bh[ch][0], bh[ch][1]);
+                    }
+                    if (k_halo) {
+                        mma_tf32(C[m][1], al, bh[1][0], bh[1][1]);
+                        mma_tf32(C[m][1], ah, bl[1][0], bl[1][1]);
+                        mma_tf32(C[m][1], ah, bh[1][0], bh[1][1]);
                     }
                 }
             }
