@@ -33,6 +33,7 @@
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "asg_common.cuh"
 #include "asg_internal.h"
@@ -1018,32 +1019,57 @@ k_deposit_mma2(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                     tf32_split(__fmul_rn(za, S.v[s8 + t][1]), bh[1][0], bl[1][0]);
                     tf32_split(__fmul_rn(zb, S.v[s8 + t + 4][1]), bh[1][1], bl[1][1]);
                 }
+                // the warp's row blocks this K step touches, both in one block
+                // of code when both do (twice the independent chains)
+                auto blocks = [&](auto use0, auto use1) {
+                    constexpr bool U[2] = {decltype(use0)::value, decltype(use1)::value};
+                    uint32_t ah[2][4], al[2][4];
 #pragma unroll
-                for (int m = 0; m < 2; ++m) {
-                    const int mb = 2 * wp + m;
-                    if (!(kinfo & (3u << (2 * mb)))) continue;
-                    uint32_t ah[4], al[4];
-                    tf32_split(__fmul_rn(xa, wa[TS + 2 * mb]), ah[0], al[0]);
-                    tf32_split(__fmul_rn(xa, wa[TS + 2 * mb + 1]), ah[1], al[1]);
-                    tf32_split(__fmul_rn(xb, wb[TS + 2 * mb]), ah[2], al[2]);
-                    tf32_split(__fmul_rn(xb, wb[TS + 2 * mb + 1]), ah[3], al[3]);
+                    for (int m = 0; m < 2; ++m) {
+                        if (!U[m]) continue;
+                        const int mb = 2 * wp + m;
+                        tf32_split(__fmul_rn(xa, wa[TS + 2 * mb]), ah[m][0], al[m][0]);
+                        tf32_split(__fmul_rn(xa, wa[TS + 2 * mb + 1]), ah[m][1], al[m][1]);
+                        tf32_split(__fmul_rn(xb, wb[TS + 2 * mb]), ah[m][2], al[m][2]);
+                        tf32_split(__fmul_rn(xb, wb[TS + 2 * mb + 1]), ah[m][3], al[m][3]);
+                    }
                     if (k_main) {
 #pragma unroll
-                        for (int ch = 0; ch < NCH; ++ch)
-                            if (!(NCH > 1 && ch == 1)) mma_tf32(C[m][ch], al, bh[ch][0], bh[ch][1]);
+                        for (int m = 0; m < 2; ++m)
 #pragma unroll
-                        for (int ch = 0; ch < NCH; ++ch)
-                            if (!(NCH > 1 && ch == 1)) mma_tf32(C[m][ch], ah, bl[ch][0], bl[ch][1]);
+                            for (int ch = 0; ch < NCH; ++ch)
+                                if (U[m] && !(NCH > 1 && ch == 1))
+                                    mma_tf32(C[m][ch], al[m], bh[ch][0], bh[ch][1]);
 #pragma unroll
-                        for (int ch = 0; ch < NCH; ++ch)
-                            if (!(NCH > 1 && ch == 1)) mma_tf32(C[m][ch], ah, bh[ch][0], bh[ch][1]);
+                        for (int m = 0; m < 2; ++m)
+#pragma unroll
+                            for (int ch = 0; ch < NCH; ++ch)
+                                if (U[m] && !(NCH > 1 && ch == 1))
+                                    mma_tf32(C[m][ch], ah[m], bl[ch][0], bl[ch][1]);
+#pragma unroll
+                        for (int m = 0; m < 2; ++m)
+#pragma unroll
+                            for (int ch = 0; ch < NCH; ++ch)
+                                if (U[m] && !(NCH > 1 && ch == 1))
+                                    mma_tf32(C[m][ch], ah[m], bh[ch][0], bh[ch][1]);
                     }
                     if (k_halo) {
-                        mma_tf32(C[m][1], al, bh[1][0], bh[1][1]);
-                        mma_tf32(C[m][1], ah, bl[1][0], bl[1][1]);
-                        mma_tf32(C[m][1], ah, bh[1][0], bh[1][1]);
+#pragma unroll
+                        for (int m = 0; m < 2; ++m)
+                            if (U[m]) mma_tf32(C[m][1], al[m], bh[1][0], bh[1][1]);
+#pragma unroll
+                        for (int m = 0; m < 2; ++m)
+                            if (U[m]) mma_tf32(C[m][1], ah[m], bl[1][0], bl[1][1]);
+#pragma unroll
+                        for (int m = 0; m < 2; ++m)
+                            if (U[m]) mma_tf32(C[m][1], ah[m], bh[1][0], bh[1][1]);
                     }
-                }
+                };
+                const bool r0 = (kinfo & (3u << (4 * wp))) != 0;
+                const bool r1 = (kinfo & (3u << (4 * wp + 2))) != 0;
+                if (r0 && r1) blocks(std::true_type{}, std::true_type{});
+                else if (r0) blocks(std::true_type{}, std::false_type{});
+                else blocks(std::false_type{}, std::true_type{});
             }
             // ---- flush the fragments into the lane's sums (every chunk of 64 pairs) ----
 #pragma unroll
