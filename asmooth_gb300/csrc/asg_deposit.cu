@@ -46,6 +46,9 @@ constexpr int DEP_THREADS = 256;   // threads of the tile-merge CTA
 constexpr int SEG_DEFAULT = 4096;  // pairs per work item unless DepositParams::seg says otherwise
 constexpr int PW = 9;              // partial words per cell
 constexpr int IMG_BITS = 5;        // periodic images per pair: up to 3 x 3 x 3
+// key bits of the image index: none without periodic images (every pair is
+// image 0), so the pair sort needs fewer passes
+__host__ __device__ inline int img_bits(const DepositParams& P) { return P.periodic ? IMG_BITS : 0; }
 constexpr unsigned FULLM = 0xffffffffu;
 
 // ---------------------------------------------------------------------------
@@ -211,7 +214,7 @@ __global__ void k_pairs(const float4* __restrict__ rec, int n, DepositParams P,
                                         const uint32_t tile = (uint32_t)J.tile_begin +
                                             (uint32_t)((tz * J.tiles[1] + ty) * J.tiles[0] + tx);
                                         if (o < cap) {
-                                            keys[o] = (tile << IMG_BITS) | combo;
+                                            keys[o] = (tile << img_bits(P)) | combo;
                                             vals[o] = i;
                                         } else {
                                             atomicOr(err, ERR_CAP);
@@ -240,15 +243,15 @@ __global__ void k_pad_pairs(uint32_t* __restrict__ keys, int* __restrict__ vals,
 
 // first pair and pair count of every tile (sorted keys; empty tiles stay 0;
 // tiles >= total_tiles are padding)
-__global__ void k_tile_bounds(const uint32_t* __restrict__ keys, int np, int total_tiles,
+__global__ void k_tile_bounds(const uint32_t* __restrict__ keys, int np, int total_tiles, int ib,
                               uint32_t* __restrict__ tstart, uint32_t* __restrict__ tcount)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= np) return;
-    const uint32_t t = keys[j] >> IMG_BITS;
+    const uint32_t t = keys[j] >> ib;
     if (t >= (uint32_t)total_tiles) return;
-    if (j == 0 || (keys[j - 1] >> IMG_BITS) != t) tstart[t] = (uint32_t)j;
-    if (j == np - 1 || (keys[j + 1] >> IMG_BITS) != t) tcount[t] = (uint32_t)j + 1;  // end for now
+    if (j == 0 || (keys[j - 1] >> ib) != t) tstart[t] = (uint32_t)j;
+    if (j == np - 1 || (keys[j + 1] >> ib) != t) tcount[t] = (uint32_t)j + 1;  // end for now
 }
 
 // tcount: end -> count; nitems: seg-pair work items per tile (at least one)
@@ -439,7 +442,7 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                 const int j = c0 + lane;
                 if (j < j1) {
                     const int i = pvals[j];
-                    const int combo = (int)(pkeys[j] & ((1u << IMG_BITS) - 1u));
+                    const int combo = (int)(pkeys[j] & ((1u << img_bits(P)) - 1u));
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
                     load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
@@ -708,7 +711,7 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                 for (int k = 0; k < 3 * TS; ++k) wl[k] = 0.f;
                 if (j < j1) {
                     const int i = pvals[j];
-                    const int combo = (int)(pkeys[j] & ((1u << IMG_BITS) - 1u));
+                    const int combo = (int)(pkeys[j] & ((1u << img_bits(P)) - 1u));
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
                     load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
@@ -937,7 +940,7 @@ k_deposit_mma2(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                 uint32_t info = 0;
                 if (j < j1) {
                     const int i = pvals[j];
-                    const int combo = (int)(pkeys[j] & ((1u << IMG_BITS) - 1u));
+                    const int combo = (int)(pkeys[j] & ((1u << img_bits(P)) - 1u));
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
                     load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
@@ -1236,11 +1239,11 @@ size_t deposit_tile_bytes(int total_tiles)
     return 4 * T1 * 3 + scan_temp_bytes(T1) + 256;
 }
 
-static int key_bits(int total_tiles)
+static int key_bits(int total_tiles, int ib)
 {
     int b = 0;
     while ((1 << b) < total_tiles) ++b;
-    return b + IMG_BITS;
+    return b + ib;
 }
 
 // the default deposit engine: 2 the tensor cores with the two warps of a CTA
@@ -1303,17 +1306,18 @@ void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t
     count_launches(1);
     if (padded && npairs > 0) {  // npairs is the capacity; the count itself is pcount[n]
         k_pad_pairs<<<(npairs + 255) / 256, 256, 0, s>>>(w.keys0, w.vals0, w.pcount + n, npairs,
-                                                          (uint32_t)T << IMG_BITS);
+                                                          (uint32_t)T << img_bits(p));
         count_launches(1);
     }
     const int cur = radix_sort32(w.keys0, w.vals0, w.keys1, w.vals1, (int)npairs,
-                                 key_bits(padded ? T + 1 : T), w.sort_tmp, s);
+                                 key_bits(padded ? T + 1 : T, img_bits(p)), w.sort_tmp, s);
     const uint32_t* keys = cur ? w.keys1 : w.keys0;
     const int* vals = cur ? w.vals1 : w.vals0;
     cudaMemsetAsync(w.tstart, 0, 4 * (size_t)T, s);
     cudaMemsetAsync(w.tcount, 0, 4 * (size_t)T, s);
     if (npairs > 0) {
-        k_tile_bounds<<<(npairs + 255) / 256, 256, 0, s>>>(keys, (int)npairs, T, w.tstart, w.tcount);
+        k_tile_bounds<<<(npairs + 255) / 256, 256, 0, s>>>(keys, (int)npairs, T, img_bits(p), w.tstart,
+                                                           w.tcount);
         count_launches(1);
     }
     k_tile_items<<<(T + 1 + 255) / 256, 256, 0, s>>>(w.tstart, w.tcount, T, p.seg, w.item_off);

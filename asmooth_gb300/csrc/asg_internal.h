@@ -129,7 +129,7 @@ struct DepositScratch {
     float4* rec;          // [2n] x', y', z', h (-h: halo channel, 0: skipped) | dens, v
     uint32_t* pcount;     // [n+1] pairs per particle, then their exclusive scan
     void* scan_tmp_n;     // scan scratch for n+1 entries
-    uint32_t* keys0;      // [npairs] tile << 5 | image, ping-pong with keys1
+    uint32_t* keys0;      // [npairs] tile << 5 | image (periodic), else tile; ping-pong with keys1
     uint32_t* keys1;
     int* vals0;           // [npairs] particle (sorted position), ping-pong with vals1
     int* vals1;
