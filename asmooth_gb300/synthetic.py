@@ -158,6 +158,66 @@ def nfw_cube(n: int, boxsize: float, seed: int, frac_halo: float = 0.7,
     return x, v
 
 
+def nfw_cube_device(n: int, boxsize: float, seed: int, frac_halo: float = 0.7,
+                    n_halos: int = 5000, m_range=(1e2, 1e5), c_range=(4.0, 12.0),
+                    device: str = "cuda"):
+    """``nfw_cube``'s model drawn with torch's generator on the device: the
+    same halo masses, concentrations, radii and directions by the same
+    formulas, in seconds for 512^3 particles where the numpy version takes
+    minutes.  The particles differ from ``nfw_cube``'s for the same seed.
+    Returns float32 (n, 3) device tensors x in [0, boxsize) and v."""
+    import math
+
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    f64 = dict(dtype=torch.float64, device=device)
+
+    def uni(shape, lo, hi):
+        return torch.empty(shape, **f64).uniform_(lo, hi, generator=g)
+
+    n_h = int(round(n * frac_halo))
+    n_u = n - n_h
+    mass = torch.exp(uni(n_halos, math.log(m_range[0]), math.log(m_range[1])))
+    counts = torch.floor(mass / mass.sum() * n_h).to(torch.int64)
+    short = n_h - int(counts.sum())
+    if short > 0:
+        counts[torch.argsort(-mass)[:short]] += 1
+    conc = uni(n_halos, c_range[0], c_range[1])
+    r_vir = (3.0 * counts.double() / (4.0 * math.pi * 200.0 / 8.0)) ** (1.0 / 3.0)
+    centres = uni((n_halos, 3), 0.0, boxsize)
+    owner = torch.repeat_interleave(torch.arange(n_halos, device=device), counts)
+    cc = conc[owner]
+    target = uni(owner.numel(), 0.0, 1.0) * (torch.log1p(cc) - cc / (1.0 + cc))
+    lo, hi = torch.zeros_like(cc), cc.clone()
+    for _ in range(60):  # bisection of m(x) = target, as _nfw_inverse
+        mid = 0.5 * (lo + hi)
+        below = (torch.log1p(mid) - mid / (1.0 + mid)) < target
+        lo = torch.where(below, mid, lo)
+        hi = torch.where(below, hi, mid)
+    r = 0.5 * (lo + hi) * (r_vir[owner] / cc)
+    del lo, hi, target, cc
+    d = torch.randn((owner.numel(), 3), generator=g, **f64)
+    d /= torch.linalg.norm(d, dim=1, keepdim=True)
+    x = torch.cat([uni((n_u, 3), 0.0, boxsize), centres[owner] + d * r[:, None]])
+    del d, r, owner
+    x = torch.remainder(x, boxsize).float()
+    x[x >= boxsize] = 0.0
+    for _ in range(100):  # re-draw exact duplicates, as _dedup
+        _, inv, cnt = torch.unique(x.view(torch.int32), dim=0, return_inverse=True,
+                                   return_counts=True)
+        dup = cnt[inv] > 1
+        if not bool(dup.any()):
+            break
+        first = torch.full((cnt.numel(),), x.shape[0], dtype=torch.int64, device=device)
+        first.scatter_reduce_(0, inv, torch.arange(x.shape[0], device=device), "amin")
+        dup[first] = False
+        x[dup] = uni((int(dup.sum()), 3), 0.0, boxsize).float()
+    v = torch.randn((n, 3), generator=g, dtype=torch.float32, device=device)
+    return x.contiguous(), v
+
+
 def add_periodic_shell(x: np.ndarray, v: np.ndarray, boxsize: float,
                        buffer: float) -> Cube:
     """One-rank ``exchange_buffer`` + ``remove_extra_particles`` (see module doc)."""

@@ -468,6 +468,63 @@ def run_ours(args):
         fof = {"ll": 0.4, "groups": ng, "ms": statistics.median(ms_f),
                "particles_per_s": n / (statistics.median(ms_f) * 1e-3)}
 
+    # the 512^3 cube: generated on the device (the same NFW model as the numpy
+    # generator, torch's random stream), its periodic shell built on the
+    # device; each step loads the cube with its shell, then kNN + dens and the
+    # three meshes; then GPU FOF on the loaded set
+    big = None
+    if not args.no_big and world == 1 and args.workload == "cfg2":
+        xb, vb = syn.nfw_cube_device(512 ** 3, 1024.0, 5, n_halos=20000)
+        bncs5 = (128, 256, 512)
+        ctx5 = api.Context(local)
+        s5 = torch.cuda.ExternalStream(ctx5.stream)
+        nb = [0, 0]
+
+        def step5():
+            nb[:] = ctx5.load_periodic_cube_device(xb.data_ptr(), 512 ** 3, 1024.0, 8.0 / 1024.0,
+                                                   v_ptr=vb.data_ptr())
+            ctx5.run_neighbor_search()
+            ctx5.run_deposit(1024.0, bncs5, sign=-1)
+
+        step5()
+        torch.cuda.synchronize()
+        ctx5.set_timing(True)
+        ms5 = []
+        for _ in range(3):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s5)
+            step5()
+            e1.record(s5)
+            e1.synchronize()
+            ms5.append(e0.elapsed_time(e1))
+        ph5 = {k: v / 3 for k, v in ctx5.phase_ms().items() if v}
+        ctx5.set_timing(False)
+        ng5 = ctx5.run_fof(0.4)
+        msf5 = []
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s5)
+            ng5 = ctx5.run_fof(0.4)
+            e1.record(s5)
+            e1.synchronize()
+            msf5.append(e0.elapsed_time(e1))
+        m5 = statistics.median(ms5)
+        big = {"workload": "512^3 particles, side 1024, 20000 NFW halos drawn on the device, "
+                           "8-unit periodic shell built on the device, k=32, nc=128,256,512, "
+                           "plain FP32 form",
+               "n_with_shell": nb[0], "n_local": nb[1],
+               "value": nb[1] / (m5 * 1e-3), "unit": "particles/s", "ms_per_step": m5,
+               "steps": 3, "step": "shell + index + kNN + dens + three meshes",
+               "phase_ms_per_step": ph5,
+               "fof": {"ll": 0.4, "groups": ng5, "ms": statistics.median(msf5),
+                       "particles_per_s": nb[0] / (statistics.median(msf5) * 1e-3)}}
+        ctx5.close()
+        del xb, vb
+
     # mixed-precision form: positions as int32 cell index + uint16 offsets in
     # 4-unit cells, decoded on the device, then the same FP32 path
     mixed = None
@@ -595,6 +652,8 @@ def run_ours(args):
         line["mixed"] = mixed
     if fof:
         line["fof"] = fof
+    if big:
+        line["cube_512"] = big
     if batch:
         line["batch"] = batch
     if cpu:
@@ -623,6 +682,8 @@ def main():
                          "cfg5: the 512^3 cube")
     ap.add_argument("--no-fof", action="store_true",
                     help="skip timing GPU FOF (linking length 0.4) on the loaded cube")
+    ap.add_argument("--no-big", action="store_true",
+                    help="skip the 512^3 cube (device-generated) and its FOF")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched form (27 cubes x 3 redshifts, one CUDA graph)")
     ap.add_argument("--batch-scale", type=int, default=1,

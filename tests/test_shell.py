@@ -31,3 +31,22 @@ def test_shell_matches_reference_exchange(L, b, n):
     # interior particles first, in input order; the same shell particles, bit for bit
     assert np.array_equal(cube.x[:n], rx[:n]) and np.array_equal(cube.v[:n], rv[:n])
     assert np.array_equal(_rows(cube.x, cube.v), _rows(rx, rv))
+
+
+def test_device_nfw_generator_matches_the_numpy_model():
+    """nfw_cube_device (the 512^3 bench cube's generator, run here on the CPU
+    device) draws the numpy generator's model: positions in [0, L), no exact
+    duplicates, and the same clustering (cell-count quantiles on a 32^3 grid
+    within 15% at the 99th and 99.9th percentiles)."""
+    torch = pytest.importorskip("torch")
+    n, L = 400_000, 128.0
+    x, v = syn.nfw_cube_device(n, L, 7, n_halos=300, device="cpu")
+    a = x.numpy()
+    assert a.shape == (n, 3) and a.dtype == np.float32 and v.shape == (n, 3)
+    assert a.min() >= 0.0 and a.max() < L
+    assert np.unique(a.view(np.dtype((np.void, 12))).ravel()).size == n
+    xn, _ = syn.nfw_cube(n, L, 7, n_halos=300)
+    qd = np.percentile(np.histogramdd(a, bins=32)[0], [99, 99.9])
+    qn = np.percentile(np.histogramdd(xn, bins=32)[0], [99, 99.9])
+    assert np.all(np.abs(qd / qn - 1.0) < 0.15)
+    assert isinstance(x, torch.Tensor)
