@@ -71,6 +71,9 @@ struct asg_ctx {
     Buf dacc, dexp;  // dens: fixed-point sums and scale exponents
     Buf blist;       // buckets each bundle's neighbour search scanned
     Buf nrec;        // tree node records (TreeView::rec)
+    Buf dep_order;   // the deposit's tile processing order and its inverse
+    std::vector<int> dep_order_key;  // the mesh sizes dep_order was made for
+    bool dep_order_on = true;        // ASG_DEPOSIT_ORDER=tile: tile order
     Buf uf, minin, mark, scan_tmp, lab_cnt, lab_scan;
     Buf halos, hcount, hmass;
     Buf totals, lohi;
@@ -457,6 +460,7 @@ int asg_create(asg_ctx** out, int device)
         const int v = std::atoi(e);
         if (v >= 1 && v <= LEAF_MAX) ctx->leaf = v;
     }
+    if (const char* e = std::getenv("ASG_DEPOSIT_ORDER")) ctx->dep_order_on = std::strcmp(e, "tile") != 0;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking);
@@ -485,7 +489,7 @@ void asg_destroy(asg_ctx* ctx)
                    &ctx->keys0, &ctx->keys1, &ctx->vals0, &ctx->vals1, &ctx->sort_tmp,
                    &ctx->pos, &ctx->vel, &ctx->igrp, &ctx->rk, &ctx->t33, &ctx->idx33,
                    &ctx->meta, &ctx->parent, &ctx->leaf_parent, &ctx->flags, &ctx->blo,
-                   &ctx->bhi, &ctx->dacc, &ctx->dexp, &ctx->blist, &ctx->nrec, &ctx->uf, &ctx->minin, &ctx->mark,
+                   &ctx->bhi, &ctx->dacc, &ctx->dexp, &ctx->blist, &ctx->nrec, &ctx->dep_order, &ctx->uf, &ctx->minin, &ctx->mark,
                    &ctx->scan_tmp, &ctx->lab_cnt, &ctx->lab_scan, &ctx->halos, &ctx->hcount,
                    &ctx->hmass, &ctx->totals, &ctx->lohi, &ctx->dep_rec, &ctx->dep_pcount,
                    &ctx->dep_tiles, &ctx->dep_counter, &ctx->dep_pairs, &ctx->dep_sort,
@@ -1084,6 +1088,22 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
         tiles += tpd * tpd * tpd;
     }
     if (int r = grow(ctx, ctx->totals, 16 * (size_t)n_nc)) return r;
+    // the tiles' processing order, cached while the meshes stay the same (a
+    // captured call without it takes the tiles in tile order: the same sums)
+    const std::vector<int> okey(ncs, ncs + n_nc);
+    if (ctx->dep_order_on && okey != ctx->dep_order_key && !cap) {
+        if (int r = grow(ctx, ctx->dep_order, 8 * (size_t)tiles)) return r;
+        std::vector<uint32_t> h(2 * (size_t)tiles);
+        deposit_tile_order(p, tiles, h.data());
+        CK(cudaMemcpyAsync(ctx->dep_order.p, h.data(), 8 * (size_t)tiles, cudaMemcpyHostToDevice,
+                           ctx->s));
+        CK(cudaStreamSynchronize(ctx->s));
+        ctx->dep_order_key = okey;
+    }
+    if (ctx->dep_order_on && okey == ctx->dep_order_key) {
+        p.order = P<uint32_t>(ctx->dep_order);
+        p.pos = p.order + tiles;
+    }
     // particle records and pair counts, then size the pair arrays
     const int n = ctx->n;
     const size_t T1 = (size_t)tiles + 1;

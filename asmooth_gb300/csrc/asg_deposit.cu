@@ -30,10 +30,13 @@
 //      segment order.
 // n, c and halo are double-float (two-sum) sums, so the per-tile FP64 totals
 // reproduce the FP64 sum of the float weights.
+#include <algorithm>
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <type_traits>
+#include <utility>
+#include <vector>
 
 #include "asg_common.cuh"
 #include "asg_internal.h"
@@ -254,15 +257,17 @@ __global__ void k_tile_bounds(const uint32_t* __restrict__ keys, int np, int tot
     if (j == np - 1 || (keys[j + 1] >> ib) != t) tcount[t] = (uint32_t)j + 1;  // end for now
 }
 
-// tcount: end -> count; nitems: seg-pair work items per tile (at least one)
+// tcount: end -> count; nitems: seg-pair work items per tile (at least one),
+// stored at the tile's slot of the processing order (DepositParams::pos)
 __global__ void k_tile_items(const uint32_t* __restrict__ tstart, uint32_t* __restrict__ tcount,
-                             int total_tiles, int seg, uint32_t* __restrict__ nitems)
+                             int total_tiles, int seg, const uint32_t* __restrict__ pos,
+                             uint32_t* __restrict__ nitems)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < total_tiles) {
         const uint32_t c = tcount[i] ? tcount[i] - tstart[i] : 0u;
         tcount[i] = c;
-        nitems[i] = max(1u, (c + (uint32_t)seg - 1) / (uint32_t)seg);
+        nitems[pos ? pos[i] : (uint32_t)i] = max(1u, (c + (uint32_t)seg - 1) / (uint32_t)seg);
     }
     if (i == total_tiles) nitems[i] = 0u;
 }
@@ -415,13 +420,14 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
             if ((uint32_t)item < total_items) tile = upper_index(item_off, total_tiles + 1, (uint32_t)item);
         }
         item = __shfl_sync(FULLM, item, 0);
-        tile = __shfl_sync(FULLM, tile, 0);
+        const int slot = __shfl_sync(FULLM, tile, 0);  // items are numbered in slot order
         if ((uint32_t)item >= total_items) break;
+        tile = P.order ? (int)P.order[slot] : slot;
         const TileGeo g = tile_geo(P, tile);
         const MeshJob& J = P.job[g.job];
         const int nc = g.nc;
-        const int seg = item - (int)item_off[tile];
-        const int nseg = (int)(item_off[tile + 1] - item_off[tile]);
+        const int seg = item - (int)item_off[slot];
+        const int nseg = (int)(item_off[slot + 1] - item_off[slot]);
         const int j0 = (int)tstart[tile] + seg * P.seg;
         const int j1 = (int)tstart[tile] + min((int)tcount[tile], (seg + 1) * P.seg);
 
@@ -442,7 +448,7 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                 const int j = c0 + lane;
                 if (j < j1) {
                     const int i = pvals[j];
-                    const int combo = (int)(pkeys[j] & ((1u << img_bits(P)) - 1u));
+                    const int combo = P.periodic ? (int)(pkeys[j] & ((1u << IMG_BITS) - 1u)) : 0;
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
                     load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
@@ -643,13 +649,14 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
             if ((uint32_t)item < total_items) tile = upper_index(item_off, total_tiles + 1, (uint32_t)item);
         }
         item = __shfl_sync(FULLM, item, 0);
-        tile = __shfl_sync(FULLM, tile, 0);
+        const int slot = __shfl_sync(FULLM, tile, 0);  // items are numbered in slot order
         if ((uint32_t)item >= total_items) break;
+        tile = P.order ? (int)P.order[slot] : slot;
         const TileGeo geo = tile_geo(P, tile);
         const MeshJob& J = P.job[geo.job];
         const int nc = geo.nc;
-        const int seg = item - (int)item_off[tile];
-        const int nseg = (int)(item_off[tile + 1] - item_off[tile]);
+        const int seg = item - (int)item_off[slot];
+        const int nseg = (int)(item_off[slot + 1] - item_off[slot]);
         const int j0 = (int)tstart[tile] + seg * P.seg;
         const int j1 = (int)tstart[tile] + min((int)tcount[tile], (seg + 1) * P.seg);
 
@@ -711,7 +718,7 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                 for (int k = 0; k < 3 * TS; ++k) wl[k] = 0.f;
                 if (j < j1) {
                     const int i = pvals[j];
-                    const int combo = (int)(pkeys[j] & ((1u << img_bits(P)) - 1u));
+                    const int combo = P.periodic ? (int)(pkeys[j] & ((1u << IMG_BITS) - 1u)) : 0;
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
                     load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
@@ -904,13 +911,14 @@ k_deposit_mma2(const float4* __restrict__ rec, DepositParams P, int total_tiles,
             S.tile = (uint32_t)it < total_items ? upper_index(item_off, total_tiles + 1, (uint32_t)it) : -1;
         }
         __syncthreads();
-        const int item = S.item, tile = S.tile;
+        const int item = S.item, slot = S.tile;  // items are numbered in slot order
         if ((uint32_t)item >= total_items) break;
+        const int tile = P.order ? (int)P.order[slot] : slot;
         const TileGeo geo = tile_geo(P, tile);
         const MeshJob& J = P.job[geo.job];
         const int nc = geo.nc;
-        const int seg = item - (int)item_off[tile];
-        const int nseg = (int)(item_off[tile + 1] - item_off[tile]);
+        const int seg = item - (int)item_off[slot];
+        const int nseg = (int)(item_off[slot + 1] - item_off[slot]);
         const int j0 = (int)tstart[tile] + seg * P.seg;
         const int j1 = (int)tstart[tile] + min((int)tcount[tile], (seg + 1) * P.seg);
 
@@ -940,7 +948,7 @@ k_deposit_mma2(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                 uint32_t info = 0;
                 if (j < j1) {
                     const int i = pvals[j];
-                    const int combo = (int)(pkeys[j] & ((1u << img_bits(P)) - 1u));
+                    const int combo = P.periodic ? (int)(pkeys[j] & ((1u << IMG_BITS) - 1u)) : 0;
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
                     load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
@@ -1175,7 +1183,8 @@ k_merge_tiles(DepositParams P, int total_tiles, const uint32_t* __restrict__ ite
 {
     __shared__ double red[2][DEP_THREADS / 32];
     const int tile = blockIdx.x;
-    const int i0 = (int)item_off[tile], i1 = (int)item_off[tile + 1];
+    const int slot = P.pos ? (int)P.pos[tile] : tile;
+    const int i0 = (int)item_off[slot], i1 = (int)item_off[slot + 1];
     if (i1 - i0 <= 1) return;
     const TileGeo g = tile_geo(P, tile);
     const MeshJob& J = P.job[g.job];
@@ -1231,6 +1240,44 @@ k_merge_tiles(DepositParams P, int total_tiles, const uint32_t* __restrict__ ite
 // host side
 // ---------------------------------------------------------------------------
 size_t deposit_prep_bytes(int n) { return 32 * (size_t)n; }
+
+// bits 0-10 of v spread to every third bit
+static uint64_t spread3_11(uint32_t v)
+{
+    uint64_t r = 0;
+    for (int b = 0; b < 11; ++b) r |= (uint64_t)((v >> b) & 1u) << (3 * b);
+    return r;
+}
+
+void deposit_tile_order(const DepositParams& p, int total_tiles, uint32_t* out)
+{
+    int ncmax = 1;
+    for (int k = 0; k < p.n_jobs; ++k) ncmax = std::max(ncmax, p.job[k].nc);
+    std::vector<std::pair<uint64_t, uint32_t>> key((size_t)total_tiles);
+    for (int k = 0; k < p.n_jobs; ++k) {
+        const MeshJob& J = p.job[k];
+        int rank = 0;  // coarser meshes first at the same place
+        for (int j = 0; j < p.n_jobs; ++j)
+            rank += p.job[j].nc < J.nc || (p.job[j].nc == J.nc && j < k);
+        // a tile's lower corner, in tiles of the finest mesh (plus half of one)
+        const double ratio = (double)ncmax / (double)J.nc;
+        const int nt = J.tiles[0] * J.tiles[1] * J.tiles[2];
+        for (int t = 0; t < nt; ++t) {
+            const int c[3] = {t % J.tiles[0], (t / J.tiles[0]) % J.tiles[1],
+                              t / (J.tiles[0] * J.tiles[1])};
+            uint64_t m = 0;
+            for (int a = 0; a < 3; ++a)
+                m |= spread3_11(std::min(2047u, (uint32_t)(c[a] * ratio + 0.5))) << a;
+            key[(size_t)(J.tile_begin + t)] = {(m << 4) | (uint64_t)rank,
+                                               (uint32_t)(J.tile_begin + t)};
+        }
+    }
+    std::sort(key.begin(), key.end());
+    for (int slot = 0; slot < total_tiles; ++slot) {
+        out[slot] = key[(size_t)slot].second;
+        out[(size_t)total_tiles + key[(size_t)slot].second] = (uint32_t)slot;
+    }
+}
 
 size_t deposit_tile_bytes(int total_tiles)
 {
@@ -1320,7 +1367,7 @@ void launch_deposit_run(int n, const DepositParams& p, int total_tiles, uint32_t
                                                            w.tcount);
         count_launches(1);
     }
-    k_tile_items<<<(T + 1 + 255) / 256, 256, 0, s>>>(w.tstart, w.tcount, T, p.seg, w.item_off);
+    k_tile_items<<<(T + 1 + 255) / 256, 256, 0, s>>>(w.tstart, w.tcount, T, p.seg, p.pos, w.item_off);
     exclusive_scan_u32(w.item_off, (size_t)T + 1, w.scan_tmp_t, s);
     cudaMemsetAsync(w.next_item, 0, sizeof(int), s);
     int dev = 0, sms = 0;

@@ -123,7 +123,17 @@ struct DepositParams {
     int seg;          // pairs per work item of the persistent deposit (tuning, > 0)
     int mma;          // the deposit engine: 1 or 2 tensor cores (one or two warps per
                       // item), 0 the CUDA cores (tuning)
+    // the order in which the persistent deposit takes the tiles (slot -> tile)
+    // and its inverse (tile -> slot), or null for tile order: tiles of every
+    // mesh sorted by position along a Morton curve, coarse before fine at the
+    // same place, so that the tiles of all meshes that read the same particle
+    // records run close together in time and find them in L2
+    const uint32_t* order;
+    const uint32_t* pos;
 };
+// the processing order above for the meshes of p (host; 2 * total tiles words:
+// order, then pos)
+void deposit_tile_order(const DepositParams& p, int total_tiles, uint32_t* out);
 // scratch of one deposit: particle records, (tile, image) pairs, work items
 struct DepositScratch {
     float4* rec;          // [2n] x', y', z', h (-h: halo channel, 0: skipped) | dens, v
