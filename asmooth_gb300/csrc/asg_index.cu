@@ -603,26 +603,50 @@ __global__ void k_tree_boxes(const float4* __restrict__ pos, const float* __rest
                              int* flags, float4* lo, float4* hi)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int4 m = meta[i];
+    const int lane = threadIdx.x & 31;
+    const bool valid = i < n - 1;
+    const int4 m = valid ? meta[i] : make_int4(0, 0, 0, 0);
     float4 l, h, l1, h1;
-    if (m.w - m.z + 1 > leaf) {
-        if (m.x >= 0 || m.y >= 0) return;  // reached by the climbs from its internal children
-        leaf_box(pos, rk, ~m.x, l, h);     // two particle children (leaf = 1 only)
-        leaf_box(pos, rk, ~m.y, l1, h1);
-        box_union(l, h, l1, h1);
-    } else {
-        const int p = parent[i];
-        if (p >= 0) {
-            const int4 mp = meta[p];
-            if (mp.w - mp.z + 1 <= leaf) return;  // inside a bucket: never read
-        }
-        leaf_box(pos, rk, m.z, l, h);
-        for (int k = m.z + 1; k <= m.w; ++k) {
-            leaf_box(pos, rk, k, l1, h1);
-            box_union(l, h, l1, h1);
+    bool start = false;  // this thread finishes node i and climbs from it
+    bool top = false;    // node i is a top bucket
+    if (valid) {
+        if (m.w - m.z + 1 > leaf) {
+            start = m.x < 0 && m.y < 0;  // two particle children (leaf = 1 only)
+            if (start) {
+                leaf_box(pos, rk, ~m.x, l, h);
+                leaf_box(pos, rk, ~m.y, l1, h1);
+                box_union(l, h, l1, h1);
+            }
+        } else {
+            const int p = parent[i];
+            top = p < 0 || meta[p].w - meta[p].z + 1 > leaf;  // not inside a larger bucket
+            start = top;
         }
     }
+    // the warp reduces its top buckets one after another, lanes over the
+    // bucket's (at most 32) contiguous particles: one coalesced load each
+    unsigned tops = __ballot_sync(0xffffffffu, top);
+    while (tops) {
+        const int src = __ffs(tops) - 1;
+        tops &= tops - 1;
+        const int first = __shfl_sync(0xffffffffu, m.z, src);
+        const int last = __shfl_sync(0xffffffffu, m.w, src);
+        float4 bl, bh;
+        leaf_box(pos, rk, min(first + lane, last), bl, bh);
+        float r[6] = {bl.x, bl.y, bl.z, bh.x, bh.y, bh.z};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int a = 0; a < 6; ++a) {
+                const float v = __shfl_xor_sync(0xffffffffu, r[a], o);
+                r[a] = a < 3 ? fminf(r[a], v) : fmaxf(r[a], v);
+            }
+        if (lane == src) {
+            l = make_float4(r[0], r[1], r[2], 0.f);
+            h = make_float4(r[3], r[4], r[5], 0.f);
+        }
+    }
+    if (!start) return;
     __stcg(&lo[i], l);
     __stcg(&hi[i], h);
     int node = parent[i];
