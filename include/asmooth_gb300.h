@@ -369,9 +369,10 @@ int asg_deposit_stats(asg_ctx* ctx, long long* pairs, long long* tiles, long lon
  * address and returns ASG_OK.  Make it on each device before reserving the
  * memory pool, and again after a cudaDeviceReset (the address kept from before
  * is stale then).  Without it the first search on a device does the same
- * set-up; make that first call before any stream capture.
- * stream may be NULL (the default stream).  The call is synchronous: it
- * returns when its work on stream is complete.  It returns ASG_ERR_CUDA, before
+ * set-up.
+ * stream may be NULL (the default stream).  The call is synchronous: it waits
+ * for its work on stream and reads the error word back before it returns, so
+ * it cannot be captured into a CUDA graph.  It returns ASG_ERR_CUDA, before
  * doing any work, when the calling thread holds an unread CUDA error from
  * earlier work (left for the caller to read). */
 #define ASG_NOALLOC_MAX_PARTICLES 32768
