@@ -437,9 +437,25 @@ def run_ours(args):
             pipes = {k: rec[k] for k in ("alu_pipe_pct_of_peak", "fma_pipe_pct_of_peak",
                                          "tensor_pipe_pct_of_peak", "issue_active_pct", "kernel",
                                          "capture") if k in rec}
+    # DRAM bytes per particle of each dominant kernel (the capture's figure)
+    # against its algorithmic bytes: kNN reads a position (16 B) and writes
+    # t33, rk and the tie flag (12 B); dens reads a position, t33, idx33 and rk
+    # (28 B) and adds into one 64-bit sum (8 B); the deposit reads a particle
+    # record (36 B) and writes the meshes (24 B per cell)
+    alg_bpp = {"knn_t33": 28.0, "dens": 36.0, "deposit": 36.0 + sum(24 * nc ** 3 for nc in ncs) / n}
+    by_kernel = {}
+    if os.path.exists(tpath):
+        tj = json.load(open(tpath))
+        for k, a_b in alg_bpp.items():
+            if k in tj:
+                by_kernel[k] = {"kernel": tj[k]["kernel"],
+                                "bytes_per_particle": tj[k]["bytes_per_particle"],
+                                "algorithmic_bytes_per_particle": a_b,
+                                "ratio": tj[k]["bytes_per_particle"] / a_b}
     hbm_alg = n * (12 + 8 + 36) + sum(24 * nc ** 3 for nc in ncs)
     roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": fp32, "unit": "TFLOP/s",
             "frac": achieved / fp32, "traffic": traffic, "pipe_utilisation_ncu": pipes,
+            "traffic_by_kernel": by_kernel,
             "peak_source": "measured FMA-chain kernel on this GPU (no FP32 figure in the peaks file)",
             "phase_ms_per_step": per_step,
             "alg_flops_per_step": alg,

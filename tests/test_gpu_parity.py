@@ -330,3 +330,22 @@ def test_deep_ties_at_33rd(gpu_ctx, oracle):
     p2 = api.make_particles(X)
     gpu_ctx.neighbor_search(p2, 0.0, 140.0)
     assert p.tobytes() == p2.tobytes()
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_deposit_tile_order_changes_no_bit(oracle, periodic, monkeypatch):
+    """The persistent deposit takes the tiles of all meshes in a Morton order
+    (ASG_DEPOSIT_ORDER=tile: tile order).  The order only changes when each
+    tile is summed, not how, so meshes and FP64 totals are bit-identical."""
+    cube, ncs = syn.make_workload("cfg2", scale=4)
+    out = {}
+    for order in ("tile", "morton"):
+        monkeypatch.setenv("ASG_DEPOSIT_ORDER", order)
+        with api.Context(0) as ctx:
+            p = api.make_particles(cube.x, cube.v)
+            ctx.neighbor_search(p, cube.left, cube.right)
+            out[order] = ctx.assign_on_meshes(p, cube.boxsize, ncs, sign=-1, periodic=periodic)
+    (m0, t0), (m1, t1) = out["tile"], out["morton"]
+    for a, b in zip(m0, m1):
+        assert np.array_equal(bits(a), bits(b))
+    assert np.array_equal(t0, t1)
