@@ -166,28 +166,51 @@ __device__ __forceinline__ float box_dist2_fast(float qx, float qy, float qz, fl
 // a point with norm2_rn <= t is never pruned (t = +inf stays +inf)
 __device__ __forceinline__ float prune_bound(float t) { return __fmul_rn(t, 1.0f + 0x1p-21f); }
 
-// the record boxes in the fast form (see rec_dist0 / rec_dist1 below)
+// A tree node record (TreeView::rec) holds in words 1-3 either a bucket's own
+// box, lo.xyz hi.x | hi.yz, or for a node with more than `leaf` particles the
+// boxes of both children as pairs, (lo0.x lo1.x lo0.y lo1.y | lo0.z lo1.z hi0.x
+// hi1.x | hi0.y hi1.y hi0.z hi1.z), so that both children are tested with
+// packed f32x2 operations.  A leaf child's box is its point, so its distance
+// equals norm2_rn to that point.
+
+// a bucket's own box in the fast form
 __device__ __forceinline__ float rec_fast0(float4 q, float4 r1, float4 r2)
 {
     return box_dist2_fast(q.x, q.y, q.z, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y);
 }
-__device__ __forceinline__ float rec_fast1(float4 q, float4 r2, float4 r3)
-{
-    return box_dist2_fast(q.x, q.y, q.z, r2.z, r2.w, r3.x, r3.y, r3.z, r3.w);
-}
-
-// a tree node record's boxes (TreeView::rec words 1-3): child 0 (or a
-// bucket's own box) and child 1; a leaf child's box is its point, so the
-// distance equals norm2_rn to that point
+// a bucket's own box, rounded as box_dist2_rn
 __device__ __forceinline__ float rec_dist0(float4 q, float4 r1, float4 r2)
 {
     return box_dist2_rn(q.x, q.y, q.z, make_float4(r1.x, r1.y, r1.z, 0.f),
                         make_float4(r1.w, r2.x, r2.y, 0.f));
 }
-__device__ __forceinline__ float rec_dist1(float4 q, float4 r2, float4 r3)
+// both children of a node in the fast form (child 0 low, child 1 high):
+// box_dist2_fast's operations on each element; qx = (q.x, q.x) and so on
+__device__ __forceinline__ f32x2 node_fast2(f32x2 qx, f32x2 qy, f32x2 qz, float4 r1, float4 r2,
+                                            float4 r3)
 {
-    return box_dist2_rn(q.x, q.y, q.z, make_float4(r2.z, r2.w, r3.x, 0.f),
-                        make_float4(r3.y, r3.z, r3.w, 0.f));
+    const f32x2 lx = sub2_rn(pack2(r1.x, r1.y), qx), hx = sub2_rn(qx, pack2(r2.z, r2.w));
+    const f32x2 ly = sub2_rn(pack2(r1.z, r1.w), qy), hy = sub2_rn(qy, pack2(r3.x, r3.y));
+    const f32x2 lz = sub2_rn(pack2(r2.x, r2.y), qz), hz = sub2_rn(qz, pack2(r3.z, r3.w));
+    const f32x2 dx = pack2(max3f(lo2(lx), lo2(hx), 0.0f), max3f(hi2(lx), hi2(hx), 0.0f));
+    const f32x2 dy = pack2(max3f(lo2(ly), lo2(hy), 0.0f), max3f(hi2(ly), hi2(hy), 0.0f));
+    const f32x2 dz = pack2(max3f(lo2(lz), lo2(hz), 0.0f), max3f(hi2(lz), hi2(hz), 0.0f));
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %1;\n\t"
+        "fma.rn.f32x2 %0, %2, %2, %0;\n\t"
+        "fma.rn.f32x2 %0, %3, %3, %0;" : "=&l"(r) : "l"(dx), "l"(dy), "l"(dz));
+    return r;
+}
+// child 0 / child 1 of a node, rounded as box_dist2_rn
+__device__ __forceinline__ float node_dist0(float4 q, float4 r1, float4 r2, float4 r3)
+{
+    return box_dist2_rn(q.x, q.y, q.z, make_float4(r1.x, r1.z, r2.x, 0.f),
+                        make_float4(r2.z, r3.x, r3.z, 0.f));
+}
+__device__ __forceinline__ float node_dist1(float4 q, float4 r1, float4 r2, float4 r3)
+{
+    return box_dist2_rn(q.x, q.y, q.z, make_float4(r1.y, r1.w, r2.y, 0.f),
+                        make_float4(r2.w, r3.y, r3.w, 0.f));
 }
 
 // double-float accumulation (Knuth two-sum): hi + lo carries ~48 bits

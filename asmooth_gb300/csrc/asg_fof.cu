@@ -85,9 +85,9 @@ k_fof_link(const float4* __restrict__ pos, TreeView t, float ll2, int* P, int* e
                 const int g = m.x >= 0 ? m.x : ~m.x;
                 // only partners with a larger sorted position are linked from q
                 const bool n0 = m.x < 0 ? (active && ~m.x > q)
-                                        : (active && g > q && rec_dist0(xq, r1, r2) <= ll2);
+                                        : (active && g > q && node_dist0(xq, r1, r2, r3) <= ll2);
                 const bool n1 = m.y < 0 ? (active && ~m.y > q)
-                                        : (active && m.w > q && rec_dist1(xq, r2, r3) <= ll2);
+                                        : (active && m.w > q && node_dist1(xq, r1, r2, r3) <= ll2);
                 const bool v0 = __any_sync(FM, n0);
                 const bool v1 = __any_sync(FM, n1);
                 if (sp + 2 > STACK_MAX) { overflow = true; break; }
@@ -261,8 +261,8 @@ k_mark_halos(const float4* __restrict__ pos, TreeView t, const float* __restrict
             const float4 c4 = make_float4(cx, cy, cz, 0.f);
             if (m.w - m.z + 1 > t.leaf) {
                 // a leaf child goes on as a one-particle bucket, tested by its norm2
-                const bool v0 = m.x < 0 || rec_dist0(c4, r1, r2v) < r2;
-                const bool v1 = m.y < 0 || rec_dist1(c4, r2v, r3) < r2;
+                const bool v0 = m.x < 0 || node_dist0(c4, r1, r2v, r3) < r2;
+                const bool v1 = m.y < 0 || node_dist1(c4, r1, r2v, r3) < r2;
                 if (sp + 2 > STACK_MAX) { overflow = true; break; }
                 if (lane == 0) {
                     if (v1) st[sp] = m.y;

@@ -693,9 +693,9 @@ __global__ void k_tree_records(const float4* __restrict__ pos, int n, int leaf,
         float4 l0, h0, l1, h1;
         if (m.x < 0) l0 = h0 = pos[~m.x]; else { l0 = lo[m.x]; h0 = hi[m.x]; }
         if (m.y < 0) l1 = h1 = pos[~m.y]; else { l1 = lo[m.y]; h1 = hi[m.y]; }
-        r1 = make_float4(l0.x, l0.y, l0.z, h0.x);
-        r2 = make_float4(h0.y, h0.z, l1.x, l1.y);
-        r3 = make_float4(l1.z, h1.x, h1.y, h1.z);
+        r1 = make_float4(l0.x, l1.x, l0.y, l1.y);  // the children's boxes as pairs
+        r2 = make_float4(l0.z, l1.z, h0.x, h1.x);
+        r3 = make_float4(h0.y, h1.y, h0.z, h1.z);
     } else {
         a = lo[i];
         b = hi[i];

@@ -96,6 +96,7 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
     if (base >= n) return;
     const int q = min(base + lane, n - 1);
     const float4 xq = pos[q];
+    const f32x2 qx = pack2(xq.x, xq.x), qy = pack2(xq.y, xq.y), qz = pack2(xq.z, xq.z);
     float a[K_NN];
 #pragma unroll
     for (int k = 0; k < K_NN; ++k) a[k] = INFINITY;
@@ -126,8 +127,8 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
                                      __float_as_int(r0.z), __float_as_int(r0.w));
             if (m.w - m.z + 1 > t.leaf) {
-                const float d0 = rec_fast0(xq, r1, r2);
-                const float d1 = rec_fast1(xq, r2, r3);
+                const f32x2 d01 = node_fast2(qx, qy, qz, r1, r2, r3);
+                const float d0 = lo2(d01), d1 = hi2(d01);
                 const float bound = prune_bound(a[K_NN - 1]);
                 // a node whose distance equals a[32] can hold a tie: visit it
                 const bool v0 = __any_sync(FULL, d0 <= bound);
@@ -171,7 +172,6 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
         // two candidates per step (their distances in packed f32x2 operations),
         // then one check: every queue holds at most KNN_QUEUE - 2 values when a
         // step begins (equal values queue too: the merge tracks ties)
-        const f32x2 qx = pack2(xq.x, xq.x), qy = pack2(xq.y, xq.y), qz = pack2(xq.z, xq.z);
         const f32x2* cx = reinterpret_cast<const f32x2*>(cand[warp][0]);
         const f32x2* cy = reinterpret_cast<const f32x2*>(cand[warp][1]);
         const f32x2* cz = reinterpret_cast<const f32x2*>(cand[warp][2]);
@@ -257,8 +257,8 @@ k_knn_ties(const float4* __restrict__ pos, TreeView t, const float* __restrict__
                 const int4 m = make_int4(__float_as_int(r0.x), __float_as_int(r0.y),
                                          __float_as_int(r0.z), __float_as_int(r0.w));
                 if (m.w - m.z + 1 > t.leaf) {
-                    const bool v0 = __any_sync(FULL, open && rec_dist0(xq, r1, r2) <= T);
-                    const bool v1 = __any_sync(FULL, open && rec_dist1(xq, r2, r3) <= T);
+                    const bool v0 = __any_sync(FULL, open && node_dist0(xq, r1, r2, r3) <= T);
+                    const bool v1 = __any_sync(FULL, open && node_dist1(xq, r1, r2, r3) <= T);
                     if (sp + 2 > STACK_MAX) { overflow = true; break; }
                     if (lane == 0) {
                         if (v1) st[sp] = m.y;
