@@ -388,15 +388,19 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
         const float4 c = pos[j];
         const float sc = __int_as_float((127 + FIX_BITS - dexp[j]) << 23);  // 2^(FIX_BITS - e_j)
         const int cj = __float_as_int(c.w);
+        const f32x2 cxy = pack2(c.x, c.y);
         float sh = 0.0f, sl = 0.0f;  // sum of the scaled weights, double-float
         while (M) {
             const int k = __ffs(M) - 1;
             M &= M - 1;
             const float4 Q = qpos[warp][k];
             const float4 A = qaux[warp][k];
-            // norm2 (nbr_search.cpp:20-25) and ker (:27-37) of (q, j), query first
-            const float dx = __fsub_rn(Q.x, c.x), dy = __fsub_rn(Q.y, c.y), dz = __fsub_rn(Q.z, c.z);
-            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            // norm2 (nbr_search.cpp:20-25) and ker (:27-37) of (q, j), query first;
+            // x and y as one packed pair (the same roundings)
+            const f32x2 dxy = sub2_rn(pack2(Q.x, Q.y), cxy);
+            const float dx = lo2(dxy), dy = hi2(dxy), dz = __fsub_rn(Q.z, c.z);
+            const f32x2 sxy = sq2_rn(dxy);
+            const float d2 = __fadd_rn(__fadd_rn(lo2(sxy), hi2(sxy)), __fmul_rn(dz, dz));
             bool member = d2 < Q.w;
             if constexpr (decltype(ties)::value) member = member || (d2 == Q.w && cj < __float_as_int(A.z));
             float w = A.y;
