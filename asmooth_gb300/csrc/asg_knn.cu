@@ -44,7 +44,7 @@ constexpr unsigned FULL = 0xffffffffu;
 // exact: the values dropped by the merge are all >= the 34th smallest t34, so
 // one of them ties the new a[32] exactly when t34 == a[32]; an earlier tie
 // survives only while a[32] is unchanged.
-__device__ __forceinline__ void knn_flush(float (&a)[K_NN], float* qb, int& qn, bool& tie_out)
+__device__ __forceinline__ void knn_flush(float (&a)[K_NN], float* qb, float*& qp, bool& tie_out)
 {
     float v[KNN_QUEUE];
 #pragma unroll
@@ -52,7 +52,7 @@ __device__ __forceinline__ void knn_flush(float (&a)[K_NN], float* qb, int& qn, 
         v[i] = qb[32 * i];
         qb[32 * i] = INFINITY;
     }
-    qn = 0;
+    qp = qb;
     knn_sort16(v);
     const float old = a[K_NN - 1];
     const float t34 = knn_merge33(a, v);
@@ -102,7 +102,7 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
     for (int k = 0; k < K_NN; ++k) a[k] = INFINITY;
     bool tie_out = false;  // a particle outside a[] has d2 == a[32]
     float* qb = &queue[warp][0][lane];
-    int qn = 0;
+    float* qp = qb;  // the lane's next free queue slot (qb + 32 x queued values)
 #pragma unroll
     for (int i = 0; i < KNN_QUEUE; ++i) qb[32 * i] = INFINITY;
     __shared__ int nlist[T33_WARPS];  // buckets scanned (kept in shared memory: registers are full)
@@ -179,13 +179,13 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             const f32x2 d2 = norm2_rn_x2(qx, qy, qz, cx[j >> 1], cy[j >> 1], cz[j >> 1]);
             const float d0 = lo2(d2), d1 = hi2(d2);
             const float top = a[K_NN - 1];
-            if (d0 <= top) qb[32 * qn++] = d0;
-            if (d1 <= top) qb[32 * qn++] = d1;
-            if (__any_sync(FULL, qn > KNN_QUEUE - 2)) knn_flush(a, qb, qn, tie_out);
+            if (d0 <= top) { *qp = d0; qp += 32; }
+            if (d1 <= top) { *qp = d1; qp += 32; }
+            if (__any_sync(FULL, qp > qb + 32 * (KNN_QUEUE - 2))) knn_flush(a, qb, qp, tie_out);
         }
         __syncwarp();
     }
-    if (__any_sync(FULL, qn > 0)) knn_flush(a, qb, qn, tie_out);
+    if (__any_sync(FULL, qp > qb)) knn_flush(a, qb, qp, tie_out);
     // every bucket any lane's final radius reaches was scanned, so the list is
     // complete for k_dens_scatter unless it overflowed or the stack did
     if (blist && lane == 0)
