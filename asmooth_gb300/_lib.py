@@ -48,6 +48,7 @@ SIGNATURES = {
     "asg_batch_create": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, C.POINTER(_vp)]),
     "asg_batch_destroy": (None, [_vp]),
     "asg_batch_set_item": (_i, [_vp, _i, _vp, _vp, _i]),
+    "asg_batch_set_item_quantised": (_i, [_vp, _i, _vp, _vp, _vp, _f, _i, _i]),
     "asg_batch_tune": (_i, [_vp, _ip, _ip]),
     "asg_batch_config": (_i, [_vp, _ip, _ip, _ip, _ip]),
     "asg_batch_set_streams": (_i, [_vp, _i]),

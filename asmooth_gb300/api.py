@@ -499,6 +499,17 @@ class Batch:
             raise ValueError("item size is fixed at creation")
         self.ctx._ok(self.lib.asg_batch_set_item(self.h, int(i), _ptr(x), _ptr(v), 0))
 
+    def set_item_quantised(self, i: int, cell: np.ndarray, off: np.ndarray,
+                           v: np.ndarray | None, cell_size: float, grid: int):
+        """Item i in the mixed-precision form (asg_batch_set_item_quantised)."""
+        cell = np.ascontiguousarray(cell, np.int32)
+        off = np.ascontiguousarray(off, np.uint16)
+        v = None if v is None else np.ascontiguousarray(v, np.float32)
+        if cell.shape != (self.n[i],) or off.shape != (self.n[i], 3):
+            raise ValueError("item size is fixed at creation")
+        self.ctx._ok(self.lib.asg_batch_set_item_quantised(self.h, int(i), _ptr(cell), _ptr(off),
+                                                           _ptr(v), float(cell_size), int(grid), 0))
+
     def set_streams(self, streams: int):
         self.ctx._ok(self.lib.asg_batch_set_streams(self.h, int(streams)))
 

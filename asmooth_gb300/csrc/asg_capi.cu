@@ -1639,6 +1639,12 @@ struct asg_batch {
     size_t n_total = 0, mesh_words = 0;
     int max_n = 0;
     Buf in_x, in_v, out_rk, out_dens, out_mesh, out_tot;
+    // mixed-precision items: int32 cell index and 3 x uint16 offsets per
+    // particle (allocated with the first such item); quant[i] > 0 is item i's
+    // grid, with its cell size in cell_size[i]
+    Buf in_cell, in_off;
+    std::vector<int> quant;
+    std::vector<float> cell_size;
     std::vector<uint32_t> cap;     // pair capacity per item (from the planning pass)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1671,9 +1677,15 @@ int batch_queue_item(asg_batch* b, asg_ctx* ctx, int i, uint32_t cap)
     ctx->n = n;
     ctx->left = b->left[(size_t)i];
     ctx->right = b->right[(size_t)i];
-    launch_unpack_soa(P<float>(b->in_x) + 3 * o, P<float>(b->in_v) + 3 * o, nullptr, nullptr, n,
-                      P<float4>(ctx->pos_in), P<float4>(ctx->vel_in), P<int>(ctx->igrp_in),
-                      P<float>(ctx->rk_in), ctx->d_err, ctx->s);
+    if (b->quant[(size_t)i] > 0)
+        launch_unpack_quant(P<int>(b->in_cell) + o, P<uint16_t>(b->in_off) + 3 * o,
+                            P<float>(b->in_v) + 3 * o, n, b->quant[(size_t)i], ctx->left,
+                            b->cell_size[(size_t)i], P<float4>(ctx->pos_in), P<float4>(ctx->vel_in),
+                            P<int>(ctx->igrp_in), P<float>(ctx->rk_in), ctx->d_err, ctx->s);
+    else
+        launch_unpack_soa(P<float>(b->in_x) + 3 * o, P<float>(b->in_v) + 3 * o, nullptr, nullptr,
+                          n, P<float4>(ctx->pos_in), P<float4>(ctx->vel_in), P<int>(ctx->igrp_in),
+                          P<float>(ctx->rk_in), ctx->d_err, ctx->s);
     launch_space_keys(P<float4>(ctx->pos_in), n, ctx->left, ctx->right, nullptr, 0,
                   P<uint64_t>(ctx->keys0), P<int>(ctx->vals0), ctx->s);
     build_index(ctx);
@@ -1809,6 +1821,8 @@ int asg_batch_create(asg_ctx* ctx, int n_items, const int* np, const int* np_loc
         b->left.push_back(left[i]);
         b->right.push_back(right[i]);
         b->box.push_back(boxsize[i]);
+        b->quant.push_back(0);
+        b->cell_size.push_back(0.0f);
         b->off.push_back(b->n_total);
         b->n_total += (size_t)np[i];
         b->max_n = std::max(b->max_n, np[i]);
@@ -1847,7 +1861,8 @@ void asg_batch_destroy(asg_batch* b)
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->s);
     batch_drop_graph(b);
-    for (Buf* x : {&b->in_x, &b->in_v, &b->out_rk, &b->out_dens, &b->out_mesh, &b->out_tot})
+    for (Buf* x : {&b->in_x, &b->in_v, &b->in_cell, &b->in_off, &b->out_rk, &b->out_dens,
+                   &b->out_mesh, &b->out_tot})
         if (x->p) cudaFree(x->p);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
@@ -1890,10 +1905,35 @@ int asg_batch_set_item(asg_batch* b, int item, const float* x, const float* v, i
     if (!b || !x || item < 0 || item >= b->n_items) return ASG_ERR_ARG;
     asg_ctx* ctx = b->ctx;
     CK(cudaSetDevice(ctx->device));
+    if (b->quant[(size_t)item] != 0) batch_drop_graph(b);  // the item's unpack kernel changes
+    b->quant[(size_t)item] = 0;
     const size_t o = b->off[(size_t)item], bytes = 12 * (size_t)b->np[(size_t)item];
     const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     CK(cudaMemcpyAsync(P<float>(b->in_x) + 3 * o, x, bytes, kind, ctx->s));
     if (v) CK(cudaMemcpyAsync(P<float>(b->in_v) + 3 * o, v, bytes, kind, ctx->s));
+    CK(cudaStreamSynchronize(ctx->s));
+    return ASG_OK;
+}
+
+int asg_batch_set_item_quantised(asg_batch* b, int item, const int* cell, const uint16_t* off,
+                                 const float* v, float cell_size, int grid, int device_ptrs)
+{
+    if (!b || !cell || !off || item < 0 || item >= b->n_items) return ASG_ERR_ARG;
+    asg_ctx* ctx = b->ctx;
+    const size_t i = (size_t)item;
+    if (int r = check_quant(ctx, grid, cell_size, b->left[i], b->right[i])) return r;
+    CK(cudaSetDevice(ctx->device));
+    if (int r = grow(ctx, b->in_cell, 4 * b->n_total)) return r;
+    if (int r = grow(ctx, b->in_off, 6 * b->n_total)) return r;
+    if (b->quant[i] != grid || b->cell_size[i] != cell_size) batch_drop_graph(b);
+    b->quant[i] = grid;
+    b->cell_size[i] = cell_size;
+    const size_t o = b->off[i], np = (size_t)b->np[i];
+    const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    CK(cudaMemcpyAsync(P<int>(b->in_cell) + o, cell, 4 * np, kind, ctx->s));
+    CK(cudaMemcpyAsync(P<uint16_t>(b->in_off) + 3 * o, off, 6 * np, kind, ctx->s));
+    if (v) CK(cudaMemcpyAsync(P<float>(b->in_v) + 3 * o, v, 12 * np, kind, ctx->s));
+    else CK(cudaMemsetAsync(P<float>(b->in_v) + 3 * o, 0, 12 * np, ctx->s));
     CK(cudaStreamSynchronize(ctx->s));
     return ASG_OK;
 }

@@ -301,6 +301,13 @@ void asg_batch_destroy(asg_batch* batch);
 /* Item positions x (np*3) and velocities v (np*3, may be NULL = 0), host or
  * device pointers. */
 int asg_batch_set_item(asg_batch* batch, int item, const float* x, const float* v, int device_ptrs);
+/* The mixed-precision form of an item (the batched asg_smooth_quantised):
+ * cell (np int32 cell indices) and off (np*3 uint16 offsets) as for
+ * asg_load_particles_quantised, in cells of side cell_size on a grid^3 grid
+ * from the item's left; v as above.  The item keeps this form until
+ * asg_batch_set_item gives it FP32 positions again. */
+int asg_batch_set_item_quantised(asg_batch* batch, int item, const int* cell, const uint16_t* off,
+                                 const float* v, float cell_size, int grid, int device_ptrs);
 /* Run the items on `streams` concurrent streams (1..8, default 1): item i on
  * stream i % streams, each stream with its own scratch (about 300 bytes per
  * particle of the largest item), forked and joined inside the one graph. */

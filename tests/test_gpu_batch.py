@@ -133,3 +133,41 @@ def test_batch_item_vs_oracle(batch_items, oracle):
         errs = field_errors(m, m64, nc, False)
         assert max(errs.values()) <= FIELD_TOL, errs
         assert abs(t[0] - t64[0]) <= 1e-10 * t64[0]
+
+
+def test_batch_mixed_precision_items(batch_items):
+    """Items in the mixed-precision form (int32 cell + uint16 offsets, the
+    batched asg_smooth_quantised) beside FP32 items in one graph: each equals
+    the single-cube call of its form bit for bit, and an item set back to FP32
+    positions runs the FP32 path again."""
+    from asmooth_gb300.quantised import quantise
+
+    items, ncs = batch_items
+    q = [quantise(c.x, c.left, c.right, 4.0) for c in items]
+    with api.Context(0) as ctx, api.Batch(ctx, items, ncs) as b:
+        for i in (0, 3, 4):
+            cell, off, grid = q[i]
+            b.set_item_quantised(i, cell, off, items[i].v, 4.0, grid)
+        b.run()
+        b.run()
+        with api.Context(0) as ref:
+            for i, cube in enumerate(items):
+                rk, dens, meshes, tot = b.get(i)
+                if i in (0, 3, 4):
+                    cell, off, grid = q[i]
+                    rk_r, dens_r, m_r, t_r = ref.smooth_quantised(
+                        cell, off, cube.v, cube.left, cube.right, 4.0, grid, cube.boxsize, ncs, -1)
+                else:
+                    p, m_r, t_r = smooth_ref(cube, ncs)
+                    rk_r, dens_r = p["rk"], p["dens"]
+                assert np.array_equal(bits(rk), bits(rk_r))
+                assert np.array_equal(bits(dens), bits(dens_r))
+                for a, r in zip(meshes, m_r):
+                    assert np.array_equal(bits(a), bits(r))
+                assert np.array_equal(tot, t_r)
+        b.set_item(0, items[0].x, items[0].v)
+        b.run()
+        rk, _, meshes, _ = b.get(0)
+        p, m_r, _ = smooth_ref(items[0], ncs)
+        assert np.array_equal(bits(rk), bits(p["rk"]))
+        assert np.array_equal(bits(meshes[0]), bits(m_r[0]))
