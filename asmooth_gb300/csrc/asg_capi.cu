@@ -1061,6 +1061,7 @@ static int queue_deposit(asg_ctx* ctx, float boxsize, const int* ncs, int n_nc, 
     std::memset(&p, 0, sizeof(p));
     p.n_jobs = n_nc;
     p.boxsize = boxsize;
+    p.rbox = 1.0f / boxsize;  // correctly rounded (IEEE float division on the host)
     p.sign = sign;
     p.periodic = periodic ? 1 : 0;
     p.density_only = density_only ? 1 : 0;

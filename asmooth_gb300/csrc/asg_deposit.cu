@@ -143,19 +143,35 @@ __global__ void k_dep_prep(const float4* __restrict__ pos, const float4* __restr
     rec[2 * (size_t)i + 1] = make_float4(v.w, v.x, v.y, v.z);
 }
 
+// a / L rounded to nearest, given rL = 1/L rounded to nearest: q = RN(a rL) is
+// within one ulp of a/L, the residual a - q L is exact as one FMA, and
+// RN(q + residual * rL) is the correctly rounded quotient (Markstein's theorem:
+// P. W. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Develop. 34(1), 1990), for quotients
+// and residuals clear of underflow, as the cell edges here are (|a| is a
+// position plus or minus a smoothing length, L a box side).  Three operations
+// instead of a full division; for a power-of-two L the quotient is exact and
+// the residual zero.
+__device__ __forceinline__ float div_rn_by(float a, float L, float rL)
+{
+    const float q = __fmul_rn(a, rL);
+    const float r = __fmaf_rn(-q, L, a);
+    return __fmaf_rn(r, rL, q);
+}
+
 // particle i's record as the deposit kernels use it: A = (x', 1/h), B = ((x'-h)/L,
 // dens), Cc = ((x'+h)/L, vx), D = (vy, vz, flags)
 __device__ __forceinline__ void load_dep_rec(const float4* __restrict__ rec, int i, float L,
-                                             float4& A, float4& B, float4& Cc, float4& D)
+                                             float rL, float4& A, float4& B, float4& Cc, float4& D)
 {
     const float4 a = rec[2 * (size_t)i], b = rec[2 * (size_t)i + 1];
     const float h = fabsf(a.w);
     const int flags = (a.w < 0.0f ? FLAG_HALO : 0) | (h > 0.0f ? 0 : FLAG_SKIP);
     A = make_float4(a.x, a.y, a.z, __fdiv_rn(1.0f, h));
-    B = make_float4(__fdiv_rn(__fsub_rn(a.x, h), L), __fdiv_rn(__fsub_rn(a.y, h), L),
-                    __fdiv_rn(__fsub_rn(a.z, h), L), b.x);
-    Cc = make_float4(__fdiv_rn(__fadd_rn(a.x, h), L), __fdiv_rn(__fadd_rn(a.y, h), L),
-                     __fdiv_rn(__fadd_rn(a.z, h), L), b.y);
+    B = make_float4(div_rn_by(__fsub_rn(a.x, h), L, rL), div_rn_by(__fsub_rn(a.y, h), L, rL),
+                    div_rn_by(__fsub_rn(a.z, h), L, rL), b.x);
+    Cc = make_float4(div_rn_by(__fadd_rn(a.x, h), L, rL), div_rn_by(__fadd_rn(a.y, h), L, rL),
+                     div_rn_by(__fadd_rn(a.z, h), L, rL), b.y);
     D = make_float4(b.z, b.w, __int_as_float(flags), 0.0f);
 }
 
@@ -180,7 +196,7 @@ __global__ void k_pairs(const float4* __restrict__ rec, int n, DepositParams P,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 a, b, c, d;
-    load_dep_rec(rec, i, P.boxsize, a, b, c, d);
+    load_dep_rec(rec, i, P.boxsize, P.rbox, a, b, c, d);
     const int flags = __float_as_int(d.z);
     uint32_t cnt = 0;
     uint32_t o = EMIT ? offs[i] : 0u;
@@ -451,7 +467,7 @@ k_deposit_items(const float4* __restrict__ rec, DepositParams P, int total_tiles
                     const int combo = P.periodic ? (int)(pkeys[j] & ((1u << IMG_BITS) - 1u)) : 0;
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
-                    load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
+                    load_dep_rec(rec, i, P.boxsize, P.rbox, A, B, Cc, D);
                     const float xs[3] = {A.x, A.y, A.z};
                     const float lo[3] = {B.x, B.y, B.z};
                     const float hi[3] = {Cc.x, Cc.y, Cc.z};
@@ -721,7 +737,7 @@ k_deposit_mma(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                     const int combo = P.periodic ? (int)(pkeys[j] & ((1u << IMG_BITS) - 1u)) : 0;
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
-                    load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
+                    load_dep_rec(rec, i, P.boxsize, P.rbox, A, B, Cc, D);
                     const float xs[3] = {A.x, A.y, A.z};
                     const float lo[3] = {B.x, B.y, B.z};
                     const float hi[3] = {Cc.x, Cc.y, Cc.z};
@@ -951,7 +967,7 @@ k_deposit_mma2(const float4* __restrict__ rec, DepositParams P, int total_tiles,
                     const int combo = P.periodic ? (int)(pkeys[j] & ((1u << IMG_BITS) - 1u)) : 0;
                     const int dk[3] = {combo % 3, (combo / 3) % 3, combo / 9};
                     float4 A, B, Cc, D;
-                    load_dep_rec(rec, i, P.boxsize, A, B, Cc, D);
+                    load_dep_rec(rec, i, P.boxsize, P.rbox, A, B, Cc, D);
                     const float xs[3] = {A.x, A.y, A.z};
                     const float lo[3] = {B.x, B.y, B.z};
                     const float hi[3] = {Cc.x, Cc.y, Cc.z};

@@ -116,6 +116,7 @@ struct DepositParams {
     int n_jobs;
     MeshJob job[MAX_MESHES];
     float boxsize;
+    float rbox;       // 1/boxsize rounded to nearest (for div_rn_by)
     int sign;
     int periodic;
     float offset[3];  // periodic: rank cube offset
