@@ -167,7 +167,7 @@ __device__ __forceinline__ void load_dep_rec(const float4* __restrict__ rec, int
     const float4 a = rec[2 * (size_t)i], b = rec[2 * (size_t)i + 1];
     const float h = fabsf(a.w);
     const int flags = (a.w < 0.0f ? FLAG_HALO : 0) | (h > 0.0f ? 0 : FLAG_SKIP);
-    A = make_float4(a.x, a.y, a.z, __fdiv_rn(1.0f, h));
+    A = make_float4(a.x, a.y, a.z, __frcp_rn(h));  // 1/h correctly rounded
     B = make_float4(div_rn_by(__fsub_rn(a.x, h), L, rL), div_rn_by(__fsub_rn(a.y, h), L, rL),
                     div_rn_by(__fsub_rn(a.z, h), L, rL), b.x);
     Cc = make_float4(div_rn_by(__fadd_rn(a.x, h), L, rL), div_rn_by(__fadd_rn(a.y, h), L, rL),

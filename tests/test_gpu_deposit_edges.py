@@ -123,3 +123,37 @@ def test_deposit_edges(gpu_ctx, oracle, mode, sign, nc):
     e64, _ = oracle_mesh(oracle, mode, x, v, dens, rk, igrp, nc, sign, float_weights=False)
     errs = field_errors(got, e64, nc, mode == "density")
     assert max(errs.values()) <= FIELD_TOL, errs
+
+
+@pytest.mark.parametrize("box,nc", [(100.1, 24), (333.3, 37)])
+def test_deposit_box_side_not_a_power_of_two(gpu_ctx, oracle, box, nc):
+    """The normalised cell-range edges (x -+ h) / L (coarse_mesh.cpp:72-77) on a
+    box side that is not a power of two, where the quotient rounds: particles
+    on and next to every cell edge, supports ending on edges.  The cells each
+    particle reaches, and so every cell's sum, match the oracle (FP64 sums of
+    the library's weights to DEP_TOL, FP64 totals to 1e-12)."""
+    rng = np.random.default_rng(5)
+    n = 600
+    dx = np.float32(np.float32(box) / np.float32(nc))
+    edges = np.arange(nc + 1, dtype=np.float32) * dx
+    x = rng.choice(edges, (n, 3)).astype(np.float32)
+    x += rng.choice(np.float32([-1e-4, 0.0, 1e-4]), (n, 3)).astype(np.float32)
+    x[:50] = rng.uniform(0, box, (50, 3)).astype(np.float32)
+    rk = (dx * rng.choice(np.float32([0.5, 1.0, 1.5, 2.0, 0.999, 3.0]), n)).astype(np.float32)
+    v = rng.normal(size=(n, 3)).astype(np.float32)
+    dens = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    igrp = rng.choice([-1, 0, 2], n).astype(np.int32)
+    p = api.make_particles(x, v, dens=dens, rk=rk, igrp=igrp)
+    m, t = gpu_ctx.assign_on_meshes(p, float(np.float32(box)), [nc], -1)
+    _, s64, t64 = oracle.assign_on_mesh(x, v, dens, rk, igrp, float(np.float32(box)), nc, -1,
+                                        float_weights=True)
+    got, nm = m[0].astype(np.float64), nc ** 3
+    # a cell below float32's normal range (a sliver of a support's edge can
+    # weigh 1e-40) is held to DEP_TOL of the smallest normal float, since a
+    # subnormal float carries fewer significant bits
+    tiny = float(np.finfo(np.float32).tiny)
+    for a, e in ((0, nm), (nm, 2 * nm), (2 * nm, 3 * nm)):
+        s = s64[a:e]
+        assert np.all(np.abs(got[a:e] - s) <= DEP_TOL * np.maximum(np.abs(s), tiny))
+    for k in range(2):
+        assert abs(t[0][k] - t64[k]) <= TOTAL_TOL * abs(t64[k])
