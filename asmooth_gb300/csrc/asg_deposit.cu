@@ -607,11 +607,14 @@ __device__ __forceinline__ uint32_t tf32_rna(float x)
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return r;
 }
-// x = hi + lo with hi, lo TF32 (hi carries x's 11 leading bits)
+// x = hi + lo: hi = x rounded to TF32 (11 significant bits), lo = x - hi
+// (exact in FP32) passed with its FP32 bits: the tensor core reads the TF32
+// part of an operand register, so lo enters truncated to 11 significant bits,
+// an error below 2^-11 |lo| <= 2^-23 |x|
 __device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo)
 {
     hi = tf32_rna(x);
-    lo = tf32_rna(__fsub_rn(x, __uint_as_float(hi)));
+    lo = __float_as_uint(__fsub_rn(x, __uint_as_float(hi)));
 }
 __device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
                                          uint32_t b1)
