@@ -282,9 +282,7 @@ int build_index(asg_ctx* ctx)
                       P<int>(ctx->leaf_parent), ctx->s);
     launch_tree_boxes(P<float4>(ctx->pos), nullptr, n, ctx->leaf, P<int4>(ctx->meta),
                       P<int>(ctx->parent), P<int>(ctx->flags), P<float4>(ctx->blo),
-                      P<float4>(ctx->bhi), ctx->s);
-    launch_tree_records(P<float4>(ctx->pos), n, ctx->leaf, P<int4>(ctx->meta), P<float4>(ctx->blo),
-                        P<float4>(ctx->bhi), P<float4>(ctx->nrec), ctx->s);
+                      P<float4>(ctx->bhi), P<float4>(ctx->nrec), ctx->s);
     phase_end(ctx);
     ctx->loaded = true;
     ctx->knn_done = false;

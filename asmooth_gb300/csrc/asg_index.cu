@@ -591,16 +591,41 @@ __device__ __forceinline__ void box_union(float4& l, float4& h, const float4& l1
     h = make_float4(fmaxf(h.x, h1.x), fmaxf(h.y, h1.y), fmaxf(h.z, h1.z), 0.f);
 }
 
+// the 64-byte record of node i (TreeView::rec): meta, then the boxes of both
+// children as coordinate pairs, or (bucket) the node's own box
+__device__ __forceinline__ void write_node_rec(float4* rec, int i, int4 m, float4 l0, float4 h0,
+                                               float4 l1, float4 h1)
+{
+    float4* r = rec + 4 * (size_t)i;
+    r[0] = make_float4(__int_as_float(m.x), __int_as_float(m.y), __int_as_float(m.z),
+                       __int_as_float(m.w));
+    r[1] = make_float4(l0.x, l1.x, l0.y, l1.y);
+    r[2] = make_float4(l0.z, l1.z, h0.x, h1.x);
+    r[3] = make_float4(h0.y, h1.y, h0.z, h1.z);
+}
+__device__ __forceinline__ void write_bucket_rec(float4* rec, int i, int4 m, float4 l, float4 h)
+{
+    float4* r = rec + 4 * (size_t)i;
+    r[0] = make_float4(__int_as_float(m.x), __int_as_float(m.y), __int_as_float(m.z),
+                       __int_as_float(m.w));
+    r[1] = make_float4(l.x, l.y, l.z, h.x);
+    r[2] = make_float4(h.y, h.z, 0.f, 0.f);
+    r[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 // Boxes of the nodes a traversal can read: the root and every child of a node
 // with more than `leaf` particles (the traversals scan smaller nodes whole and
 // never look below them).  A "top bucket" (<= leaf particles, parent larger)
 // reduces its contiguous particles directly, then climbs: a node with two
 // internal children is finished by the second arrival (atomic flag), a node
 // with one internal child by its only climber.  Unions of the same particle
-// boxes, so the boxes are the same bits as a climb from every particle.
+// boxes, so the boxes are the same bits as a climb from every particle.  With
+// rec, each finished node also gets its record (TreeView::rec): a top bucket
+// its own box, a larger node the boxes of its children, which its finisher
+// holds at that moment; a node inside a bucket is never visited and gets none.
 __global__ void k_tree_boxes(const float4* __restrict__ pos, const float* __restrict__ rk, int n,
                              int leaf, const int4* __restrict__ meta, const int* __restrict__ parent,
-                             int* flags, float4* lo, float4* hi)
+                             int* flags, float4* lo, float4* hi, float4* __restrict__ rec)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -615,6 +640,7 @@ __global__ void k_tree_boxes(const float4* __restrict__ pos, const float* __rest
             if (start) {
                 leaf_box(pos, rk, ~m.x, l, h);
                 leaf_box(pos, rk, ~m.y, l1, h1);
+                if (rec) write_node_rec(rec, i, m, l, h, l1, h1);
                 box_union(l, h, l1, h1);
             }
         } else {
@@ -647,6 +673,7 @@ __global__ void k_tree_boxes(const float4* __restrict__ pos, const float* __rest
         }
     }
     if (!start) return;
+    if (top && rec) write_bucket_rec(rec, i, m, l, h);
     __stcg(&lo[i], l);
     __stcg(&hi[i], h);
     int node = parent[i];
@@ -661,6 +688,7 @@ __global__ void k_tree_boxes(const float4* __restrict__ pos, const float* __rest
         else { l = __ldcg(&lo[mm.x]); h = __ldcg(&hi[mm.x]); }
         if (mm.y < 0) leaf_box(pos, rk, ~mm.y, l1, h1);
         else { l1 = __ldcg(&lo[mm.y]); h1 = __ldcg(&hi[mm.y]); }
+        if (rec) write_node_rec(rec, node, mm, l, h, l1, h1);
         box_union(l, h, l1, h1);
         __stcg(&lo[node], l);
         __stcg(&hi[node], h);
@@ -669,52 +697,13 @@ __global__ void k_tree_boxes(const float4* __restrict__ pos, const float* __rest
 }
 
 void launch_tree_boxes(const float4* pos, const float* rk, int n, int leaf, const int4* meta,
-                       const int* parent, int* flags, float4* lo, float4* hi, cudaStream_t s)
+                       const int* parent, int* flags, float4* lo, float4* hi, float4* rec,
+                       cudaStream_t s)
 {
     if (n <= 1) return;
     cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(n - 1), s);
-    k_tree_boxes<<<(n - 1 + 255) / 256, 256, 0, s>>>(pos, rk, n, leaf, meta, parent, flags, lo, hi);
-    count_launches(1);
-}
-
-// one 64-byte record per internal node (see TreeView::rec); a bucket nested
-// inside a larger bucket has no box and is never visited, so its record is
-// never read
-__global__ void k_tree_records(const float4* __restrict__ pos, int n, int leaf,
-                               const int4* __restrict__ meta, const float4* __restrict__ lo,
-                               const float4* __restrict__ hi, float4* __restrict__ rec)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
-    const int4 m = meta[i];
-    float4 a, b;
-    float4 r1, r2, r3 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (m.w - m.z + 1 > leaf) {
-        float4 l0, h0, l1, h1;
-        if (m.x < 0) l0 = h0 = pos[~m.x]; else { l0 = lo[m.x]; h0 = hi[m.x]; }
-        if (m.y < 0) l1 = h1 = pos[~m.y]; else { l1 = lo[m.y]; h1 = hi[m.y]; }
-        r1 = make_float4(l0.x, l1.x, l0.y, l1.y);  // the children's boxes as pairs
-        r2 = make_float4(l0.z, l1.z, h0.x, h1.x);
-        r3 = make_float4(h0.y, h1.y, h0.z, h1.z);
-    } else {
-        a = lo[i];
-        b = hi[i];
-        r1 = make_float4(a.x, a.y, a.z, b.x);
-        r2 = make_float4(b.y, b.z, 0.f, 0.f);
-    }
-    float4* r = rec + 4 * (size_t)i;
-    r[0] = make_float4(__int_as_float(m.x), __int_as_float(m.y), __int_as_float(m.z),
-                       __int_as_float(m.w));
-    r[1] = r1;
-    r[2] = r2;
-    r[3] = r3;
-}
-
-void launch_tree_records(const float4* pos, int n, int leaf, const int4* meta, const float4* lo,
-                         const float4* hi, float4* rec, cudaStream_t s)
-{
-    if (n <= 1) return;
-    k_tree_records<<<(n - 1 + 255) / 256, 256, 0, s>>>(pos, n, leaf, meta, lo, hi, rec);
+    k_tree_boxes<<<(n - 1 + 255) / 256, 256, 0, s>>>(pos, rk, n, leaf, meta, parent, flags, lo, hi,
+                                                      rec);
     count_launches(1);
 }
 

@@ -71,12 +71,11 @@ void launch_build_tree(const uint64_t* keys, int n, int4* meta, int* parent, int
                        cudaStream_t s);
 // bottom-up AABBs of the nodes a traversal with bucket size `leaf` reads (the
 // root and the children of nodes with more than leaf particles); with
-// rk != nullptr the expanded boxes [x-h', x+h']
+// rk != nullptr the expanded boxes [x-h', x+h']; rec (or null) receives
+// TreeView::rec of those nodes (4 float4 per internal node)
 void launch_tree_boxes(const float4* pos, const float* rk, int n, int leaf, const int4* meta,
-                       const int* parent, int* flags, float4* lo, float4* hi, cudaStream_t s);
-// TreeView::rec from meta and the boxes (4 float4 per internal node)
-void launch_tree_records(const float4* pos, int n, int leaf, const int4* meta, const float4* lo,
-                         const float4* hi, float4* rec, cudaStream_t s);
+                       const int* parent, int* flags, float4* lo, float4* hi, float4* rec,
+                       cudaStream_t s);
 // exclusive scan of uint32 counts (in place); temp from scan_temp_bytes
 size_t scan_temp_bytes(size_t n);
 void exclusive_scan_u32(uint32_t* data, size_t n, void* temp, cudaStream_t s);

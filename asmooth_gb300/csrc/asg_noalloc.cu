@@ -198,9 +198,7 @@ extern "C" int asg_neighbor_search_noalloc(const float* d_x, int np, float left,
     launch_build_tree(keys, np, reinterpret_cast<int4*>(b + L.meta), I(L.parent), I(L.leaf_parent),
                       s);
     launch_tree_boxes(F4(L.pos), nullptr, np, LEAF_MAX, reinterpret_cast<int4*>(b + L.meta),
-                      I(L.parent), I(L.flags), F4(L.blo), F4(L.bhi), s);
-    launch_tree_records(F4(L.pos), np, LEAF_MAX, reinterpret_cast<const int4*>(b + L.meta),
-                        F4(L.blo), F4(L.bhi), F4(L.rec), s);
+                      I(L.parent), I(L.flags), F4(L.blo), F4(L.bhi), F4(L.rec), s);
     TreeView t;
     t.n = np;
     t.leaf = LEAF_MAX;
