@@ -1282,7 +1282,7 @@ int asg_neighbor_search(asg_ctx* ctx, asg_particle* p, int np, float left, float
     return asg_store_particles(ctx, p);
 }
 
-// load for calls whose reference signature carries no cube bounds: the Morton
+// load for calls whose reference signature carries no cube bounds: the key
 // grid only orders particles, so it spans the particles' own bounding cube,
 // found on the device
 static int load_for_deposit(asg_ctx* ctx, const asg_particle* p, int np)

@@ -9,7 +9,7 @@
 // ker(p, q, 1/rk) in dens.
 //
 // Three warp-bundle kernels over the radix tree (its 64-byte node records); a
-// warp serves the 32 consecutive (Morton-ordered) particles of one bundle, one
+// warp serves the 32 consecutive (Hilbert-ordered) particles of one bundle, one
 // lane per particle, and visits a node when any lane needs it:
 //   k_knn_t33   per-lane sorted top-33 of d2 in registers, candidates queued
 //               and merged by comparator networks (asg_knn_net.cuh)
