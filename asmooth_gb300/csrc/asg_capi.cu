@@ -910,7 +910,7 @@ static int run_knn(asg_ctx* ctx)
     phase_begin(ctx, ASG_PH_DENS);
     launch_dens(P<float4>(ctx->pos), t, P<float>(ctx->t33), P<int>(ctx->idx33), P<int>(ctx->blist),
                 P<float>(ctx->rk), P<int>(ctx->dexp), P<unsigned long long>(ctx->dacc),
-                P<float4>(ctx->vel), ctx->s);
+                P<float4>(ctx->vel), ctx->d_err, ctx->s);
     phase_end(ctx);
     ctx->knn_done = true;
     return 0;

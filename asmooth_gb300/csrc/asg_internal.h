@@ -98,7 +98,7 @@ void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int
 // dexp (n ints) and acc (n uint64) are scratch; blist from launch_knn_t33 or null
 void launch_dens(const float4* pos, const TreeView& t, const float* t33, const int* idx33,
                  const int* blist, const float* rk, int* dexp, unsigned long long* acc,
-                 float4* vel, cudaStream_t s);
+                 float4* vel, int* err, cudaStream_t s);
 
 // ---- mesh deposit (asg_deposit.cu) ---------------------------------------------
 struct MeshJob {

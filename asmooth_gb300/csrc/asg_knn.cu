@@ -37,6 +37,7 @@ constexpr int KNN_WARPS = 4;
 // slot sooner (23.07 against 23.25 ms on the 256^3 step in Morton order).  The
 // batched form's autotuner picks W.
 constexpr unsigned FULL = 0xffffffffu;
+constexpr int NO_NODE = INT_MIN;  // no node: node ids are >= 0, a leaf i is ~i >= -n
 
 // Merges a lane's queued candidates (KNN_QUEUE values in shared memory, column
 // `lane`, +inf where unused) into its ascending top-33 a[] and refills the
@@ -108,14 +109,20 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
     __shared__ int nlist[T33_WARPS];  // buckets scanned (kept in shared memory: registers are full)
     if (lane == 0) nlist[warp] = 0;
 
+    // the nearer child is visited next without going through the stack; the
+    // farther one waits on it
     int* st = stk[warp];
-    if (lane == 0) st[0] = tree_root(n);
-    int sp = 1;
+    int sp = 0;
+    int next = tree_root(n);
     bool overflow = false;
-    __syncwarp();
-    while (sp > 0) {
-        const int node = st[--sp];
-        __syncwarp();
+    for (;;) {
+        int node = next;
+        next = NO_NODE;
+        if (node == NO_NODE) {
+            if (sp == 0) break;
+            node = st[--sp];
+            __syncwarp();  // every lane has read the slot before it is written again
+        }
         int first, last;
         if (node < 0) {
             first = last = ~node;
@@ -136,13 +143,13 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
                 const bool c0_near = __popc(__ballot_sync(FULL, d0 <= d1)) >= 16;
                 const int nn = c0_near ? m.x : m.y, ff = c0_near ? m.y : m.x;
                 const bool vn = c0_near ? v0 : v1, vf = c0_near ? v1 : v0;
-                if (sp + 2 > STACK_MAX) { overflow = true; break; }
-                if (lane == 0) {
-                    if (vf) st[sp] = ff;
-                    if (vn) st[sp + (vf ? 1 : 0)] = nn;
+                if (vf) {
+                    if (sp + 1 > STACK_MAX) { overflow = true; break; }
+                    if (lane == 0) st[sp] = ff;
+                    ++sp;
+                    __syncwarp();
                 }
-                sp += (vf ? 1 : 0) + (vn ? 1 : 0);
-                __syncwarp();
+                if (vn) next = nn;
                 continue;
             }
             first = m.z;
@@ -357,7 +364,7 @@ __global__ void __launch_bounds__(KNN_WARPS * 32)
 k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restrict__ t33,
                const int* __restrict__ idx33, const int* __restrict__ blist,
                const float* __restrict__ rk, const int* __restrict__ dexp,
-               unsigned long long* __restrict__ acc)
+               unsigned long long* __restrict__ acc, int* __restrict__ err)
 {
     __shared__ int stk[KNN_WARPS][STACK_MAX];
     __shared__ float4 qpos[KNN_WARPS][32];  // x, y, z, t33 of the bundle's queries
@@ -467,7 +474,10 @@ k_dens_scatter(const float4* __restrict__ pos, TreeView t, const float* __restri
             if (m.w - m.z + 1 > t.leaf) {
                 const bool v0 = __any_sync(FULL, child_dist2(pos, t, m.x, xq) <= T);
                 const bool v1 = __any_sync(FULL, child_dist2(pos, t, m.y, xq) <= T);
-                if (sp + 2 > STACK_MAX) break;  // k_knn_t33 already flagged the same tree
+                if (sp + 2 > STACK_MAX) {
+                    if (lane == 0) atomicOr(err, ERR_STACK);
+                    break;
+                }
                 if (lane == 0) {
                     if (v1) st[sp] = m.y;
                     if (v0) st[sp + (v1 ? 1 : 0)] = m.x;
@@ -522,13 +532,13 @@ void launch_knn_ties(const float4* pos, const TreeView& t, const float* t33, int
 
 void launch_dens(const float4* pos, const TreeView& t, const float* t33, const int* idx33,
                  const int* blist, const float* rk, int* dexp, unsigned long long* acc,
-                 float4* vel, cudaStream_t s)
+                 float4* vel, int* err, cudaStream_t s)
 {
     if (t.n <= 0) return;
     const int nb = (t.n + 255) / 256;
     k_dens_prep<<<nb, 256, 0, s>>>(rk, t.n, dexp, acc);
     k_dens_scatter<<<knn_blocks(t.n), KNN_WARPS * 32, 0, s>>>(pos, t, t33, idx33, blist, rk, dexp,
-                                                             acc);
+                                                             acc, err);
     k_dens_finish<<<nb, 256, 0, s>>>(acc, dexp, t.n, vel);
     count_launches(3);
 }

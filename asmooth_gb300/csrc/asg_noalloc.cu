@@ -210,7 +210,7 @@ extern "C" int asg_neighbor_search_noalloc(const float* d_x, int np, float left,
     launch_knn_ties(F4(L.pos), t, F(L.t33), I(L.idx33), 0, err, s);
     launch_check_rk(F(L.rk), np, err, s);
     launch_dens(F4(L.pos), t, F(L.t33), I(L.idx33), nullptr, F(L.rk), I(L.dexp),
-                reinterpret_cast<unsigned long long*>(b + L.dacc), F4(L.vel), s);
+                reinterpret_cast<unsigned long long*>(b + L.dacc), F4(L.vel), err, s);
     k_noalloc_store<<<(np + 255) / 256, 256, 0, s>>>(perm, F(L.rk), F4(L.vel), np, d_rk, d_dens);
     count_launches(1);
 
