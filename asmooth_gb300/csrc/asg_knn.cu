@@ -118,7 +118,8 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
     for (;;) {
         int node = next;
         next = NO_NODE;
-        if (node == NO_NODE) {
+        const bool popped = node == NO_NODE;  // else its box passed the test just now
+        if (popped) {
             if (sp == 0) break;
             node = st[--sp];
             __syncwarp();  // every lane has read the slot before it is written again
@@ -154,9 +155,9 @@ k_knn_t33(const float4* __restrict__ pos, TreeView t, float* __restrict__ t33,
             }
             first = m.z;
             last = m.w;
-            // thresholds may have shrunk since the push: re-test the bucket
-            const float db = rec_fast0(xq, r1, r2);
-            if (!__any_sync(FULL, db <= prune_bound(a[K_NN - 1]))) continue;
+            // thresholds may have shrunk since the push: re-test a popped bucket
+            if (popped && !__any_sync(FULL, rec_fast0(xq, r1, r2) <= prune_bound(a[K_NN - 1])))
+                continue;
         }
         if (blist && lane == 0) {
             const int k = nlist[warp];
