@@ -13,6 +13,8 @@
 // SO halos (mark_halo_particles, nbr_search.cpp:140-165, driven by the loop at
 // clumping_tree_main.cpp:474-485): one warp per halo walks the tree with the
 // halo's sphere; lanes test bucket particles with d2 < r*r and set igrp = -1.
+#include <climits>
+
 #include "asg_common.cuh"
 #include "asg_internal.h"
 
@@ -48,6 +50,8 @@ __device__ __forceinline__ bool uf_union(int* P, int a, int b)
     return false;
 }
 
+constexpr int NO_NODE = INT_MIN;  // no node: node ids are >= 0, a leaf i is ~i >= -n
+
 __global__ void __launch_bounds__(FOF_WARPS * 32)
 k_fof_link(const float4* __restrict__ pos, TreeView t, float ll2, int* P, int* err)
 {
@@ -62,14 +66,19 @@ k_fof_link(const float4* __restrict__ pos, TreeView t, float ll2, int* P, int* e
     const float4 xq = pos[q];
     bool bad = false;
 
+    // child 0 is visited next directly; child 1 waits on the stack
     int* st = stk[warp];
-    if (lane == 0) st[0] = tree_root(n);
-    int sp = 1;
+    int sp = 0;
+    int next = tree_root(n);
     bool overflow = false;
-    __syncwarp();
-    while (sp > 0) {
-        const int node = st[--sp];
-        __syncwarp();
+    for (;;) {
+        int node = next;
+        next = NO_NODE;
+        if (node == NO_NODE) {
+            if (sp == 0) break;
+            node = st[--sp];
+            __syncwarp();  // every lane has read the slot before it is written again
+        }
         int first, last;
         if (node < 0) {
             first = last = ~node;
@@ -90,13 +99,13 @@ k_fof_link(const float4* __restrict__ pos, TreeView t, float ll2, int* P, int* e
                                         : (active && m.w > q && node_dist1(xq, r1, r2, r3) <= ll2);
                 const bool v0 = __any_sync(FM, n0);
                 const bool v1 = __any_sync(FM, n1);
-                if (sp + 2 > STACK_MAX) { overflow = true; break; }
-                if (lane == 0) {
-                    if (v1) st[sp] = m.y;
-                    if (v0) st[sp + (v1 ? 1 : 0)] = m.x;
+                if (v1) {
+                    if (sp + 1 > STACK_MAX) { overflow = true; break; }
+                    if (lane == 0) st[sp] = m.y;
+                    ++sp;
+                    __syncwarp();
                 }
-                sp += (v0 ? 1 : 0) + (v1 ? 1 : 0);
-                __syncwarp();
+                if (v0) next = m.x;
                 continue;
             }
             first = m.z;
