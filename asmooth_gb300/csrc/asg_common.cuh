@@ -136,6 +136,22 @@ __device__ __forceinline__ float box_dist2_rn(float qx, float qy, float qz, floa
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
+// a / L rounded to nearest, given rL = 1/L rounded to nearest: q = RN(a rL) is
+// within one ulp of a/L, the residual a - q L is exact as one FMA, and
+// RN(q + residual * rL) is the correctly rounded quotient (Markstein's theorem:
+// P. W. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Develop. 34(1), 1990), for quotients
+// and residuals clear of underflow, as the cell edges here are (|a| is a
+// position plus or minus a smoothing length, L a box side).  Three operations
+// instead of a full division; for a power-of-two L the quotient is exact and
+// the residual zero.
+__device__ __forceinline__ float div_rn_by(float a, float L, float rL)
+{
+    const float q = __fmul_rn(a, rL);
+    const float r = __fmaf_rn(-q, L, a);
+    return __fmaf_rn(r, rL, q);
+}
+
 // ---- pruning-only box test --------------------------------------------------
 // max of three floats (PTX three-input max, sm_100 and later)
 __device__ __forceinline__ float max3f(float a, float b, float c)

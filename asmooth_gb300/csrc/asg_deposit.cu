@@ -143,22 +143,6 @@ __global__ void k_dep_prep(const float4* __restrict__ pos, const float4* __restr
     rec[2 * (size_t)i + 1] = make_float4(v.w, v.x, v.y, v.z);
 }
 
-// a / L rounded to nearest, given rL = 1/L rounded to nearest: q = RN(a rL) is
-// within one ulp of a/L, the residual a - q L is exact as one FMA, and
-// RN(q + residual * rL) is the correctly rounded quotient (Markstein's theorem:
-// P. W. Markstein, "Computation of elementary functions on the IBM RISC
-// System/6000 processor", IBM J. Res. Develop. 34(1), 1990), for quotients
-// and residuals clear of underflow, as the cell edges here are (|a| is a
-// position plus or minus a smoothing length, L a box side).  Three operations
-// instead of a full division; for a power-of-two L the quotient is exact and
-// the residual zero.
-__device__ __forceinline__ float div_rn_by(float a, float L, float rL)
-{
-    const float q = __fmul_rn(a, rL);
-    const float r = __fmaf_rn(-q, L, a);
-    return __fmaf_rn(r, rL, q);
-}
-
 // particle i's record as the deposit kernels use it: A = (x', 1/h), B = ((x'-h)/L,
 // dens), Cc = ((x'+h)/L, vx), D = (vy, vz, flags)
 __device__ __forceinline__ void load_dep_rec(const float4* __restrict__ rec, int i, float L,
