@@ -554,6 +554,39 @@ def run_ours(args):
         ctx5.close()
         del xb, vb
 
+    # the reference's own small case: 64^3 particles in 200 Plummer spheres
+    # plus a uniform background, side 128, nc = 32, 64 (device time per step)
+    small = None
+    if not args.no_small and world == 1 and args.workload == "cfg2":
+        c1, ncs1 = syn.make_workload("cfg1", seed=1)
+        x1 = torch.from_numpy(c1.x).cuda()
+        v1 = torch.from_numpy(c1.v).cuda()
+
+        def step1():
+            ctx.load_particles_device(x1.data_ptr(), c1.n, c1.left, c1.right, v_ptr=v1.data_ptr())
+            ctx.run_neighbor_search()
+            ctx.run_deposit(c1.boxsize, ncs1, sign=-1)
+
+        for _ in range(3):
+            step1()
+        torch.cuda.synchronize()
+        ms1 = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step1()
+            e1.record(stream)
+            e1.synchronize()
+            ms1.append(e0.elapsed_time(e1))
+        m1 = statistics.median(ms1)
+        small = {"workload": "64^3 particles, side 128, 50% in 200 Plummer spheres, 8-unit "
+                             "periodic shell, k=32, nc=32,64, plain FP32 form",
+                 "n_with_shell": int(c1.n), "n_local": int(c1.n_local),
+                 "value": c1.n_local / (m1 * 1e-3), "unit": "particles/s", "ms_per_step": m1,
+                 "steps": args.steps, "l2": "not flushed (the whole cube fits in L2)"}
+
     # mixed-precision form: positions as int32 cell index + uint16 offsets in
     # 4-unit cells, decoded on the device, then the same FP32 path
     mixed = None
@@ -707,6 +740,8 @@ def run_ours(args):
         line["fof"] = fof
     if big:
         line["cube_512"] = big
+    if small:
+        line["cube_64"] = small
     if batch:
         line["batch"] = batch
     if cpu:
@@ -735,6 +770,8 @@ def main():
                          "cfg5: the 512^3 cube")
     ap.add_argument("--no-fof", action="store_true",
                     help="skip timing GPU FOF (linking length 0.4) on the loaded cube")
+    ap.add_argument("--no-small", action="store_true",
+                    help="skip the 64^3 Plummer cube (the reference's own small case)")
     ap.add_argument("--no-big", action="store_true",
                     help="skip the 512^3 cube (device-generated) and its FOF")
     ap.add_argument("--no-batch", action="store_true",
