@@ -459,6 +459,10 @@ int asg_create(asg_ctx** out, int device)
         if (v >= 1 && v <= LEAF_MAX) ctx->leaf = v;
     }
     if (const char* e = std::getenv("ASG_DEPOSIT_ORDER")) ctx->dep_order_on = std::strcmp(e, "tile") != 0;
+    if (const char* e = std::getenv("ASG_KNN_WARPS")) {  // tuning knob: 2 or 4 warps per block
+        const int v = std::atoi(e);
+        if (v == 2 || v == 4) ctx->knn_warps = v;
+    }
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking);
